@@ -1,0 +1,359 @@
+"""Benchmark: tracking + fusion frames/s of one SLAM session on one GB300.
+
+Workload (the BASELINE metric's configuration): 640x480 RGB-D frames of the
+seeded synthetic scene (box room, 20 spheres, 10 cuboids, sigma = 1.5 mm z^2
+depth noise, 1 % dropout), 5 mm voxels, truncation 3 voxels, 2^21 hash
+slots, FP16 TSDF + u16 weight, 3-level RGB+ICP pyramid with {10,5,3} GN
+iterations.  A step is one frame of the sequence through the whole dense
+path: image and depth pyramids, raycast of the map at the previous pose,
+model pyramid, 18 Gauss-Newton iterations with the device-side FP64 solve,
+frame-step check, pose update, block allocation, visibility, integration.
+
+value: frames/s with the frame already in HBM (one device-to-device copy
+into the session plus the captured frame graph, timed with CUDA events on
+the session stream; L2 is flushed with a 256 MB write between steps, outside
+the timed events).  e2e: frames/s through the C ABI with host (pinned)
+buffers, the host-to-device upload and the pose read-back inside the timed
+region (wall clock around the synchronous process call).
+
+``--impl reference`` times the CPU restatement of the reference's path
+(the oracle built in FP32 with OpenMP on every host core) on the same
+workload, on a bounded number of frames.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "frames/sec tracking+fusion @640x480/5mm; p50/p99 frame latency at 32 sessions"
+WORKLOAD = {
+    "workload": "single-session tracking+fusion, 640x480, 5 mm voxels, seeded synthetic RGB-D sequence",
+    "width": 640, "height": 480, "voxel_m": 0.005, "trunc_m": 0.015, "hash_slots": 1 << 21,
+    "max_blocks": 1 << 18, "tsdf": "fp16+u16", "pyramid_levels": 3, "gn_iterations": [10, 5, 3],
+    "mode": "rgb+icp", "scene_seed": 1,
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_frames(n: int, w: int, h: int, seed: int):
+    from yetanotherslam_gb300 import synth
+
+    sc = synth.Scene(seed=seed)
+    return [sc.render(i, w, h) for i in range(n)]
+
+
+# algorithmic bytes per launch of each profiled stage
+def stage_bytes(stage: int, P: list[int], nvis: int, vbytes: int, P0: int) -> float:
+    if 10 <= stage < 20:  # pass A: ref invd+int (8) + cur int/gx/gy (12) + res4 (16) + 4 float4 maps (64)
+        return 100.0 * P[stage - 10]
+    if 20 <= stage < 30:  # pass B: res4 (16) + ref invd (4)
+        return 20.0 * P[stage - 20]
+    if stage == 9:  # integration: voxels read+write, depth map, keys + visible list
+        return nvis * 512 * 2 * vbytes + 4.0 * P0 + nvis * 12.0
+    return float("nan")
+
+
+STAGE_NAMES = {0: "image_pyramid", 1: "depth_pyramid", 2: "zrange", 3: "ray_march", 4: "model_pyramid",
+               5: "gn_init", 6: "finalize", 7: "allocate", 8: "visibility", 9: "integrate"}
+
+
+def stage_name(s: int) -> str:
+    if 10 <= s < 20:
+        return f"gn_pass_a_l{s - 10}"
+    if 20 <= s < 30:
+        return f"gn_pass_b_l{s - 20}"
+    return STAGE_NAMES.get(s, str(s))
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import torch
+
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import synth, _lib as L
+    import __graft_entry__
+
+    __graft_entry__.build()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    K = synth.intrinsics(W, H)
+    nframes = 1 + args.warmup + args.steps
+    frames = make_frames(nframes + 2 * args.profile_frames + 2, W, H, WORKLOAD["scene_seed"] + rank)
+
+    def new_session():
+        return rf.Session(W, H, K, hash_slots=WORKLOAD["hash_slots"], max_blocks=WORKLOAD["max_blocks"],
+                          voxel_size=WORKLOAD["voxel_m"], trunc_dist=WORKLOAD["trunc_m"],
+                          voxel_format=rf.VOXEL_F16, num_levels=3, iterations=(10, 5, 3), use_graph=True)
+
+    # ---------------- device-resident inputs (value)
+    dev_rgb = [torch.from_numpy(f.rgb).cuda() for f in frames[:nframes]]
+    dev_dep = [torch.from_numpy(f.depth.view(np.int16)).cuda() for f in frames[:nframes]]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    s = new_session()
+    stream = torch.cuda.ExternalStream(s.stream)
+    s.process(dev_rgb[0], dev_dep[0])
+    statuses = []
+    for i in range(1, 1 + args.warmup):
+        statuses.append(s.process(dev_rgb[i], dev_dep[i])[0])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    times = []
+    with ClockSampler(local) as clk:
+        for i in range(1 + args.warmup, nframes):
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.submit(dev_rgb[i], dev_dep[i])
+            e1.record(stream)
+            st, _ = s.wait()
+            statuses.append(st)
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    lat = sorted(times)
+    kernels = s.kernels_per_frame()
+
+    # ---------------- per-stage profile (eager frames, events between launches)
+    prof = {}
+    nvis = 0
+    for j in range(args.profile_frames):
+        f = frames[nframes + j]
+        ids = np.zeros(256, np.int32)
+        ms = np.zeros(256, np.float32)
+        n = C.c_int()
+        L.call("yas_session_profile_frame", s.handle, f.rgb.ctypes.data, f.depth.ctypes.data, 0,
+               ids.ctypes.data, ms.ctypes.data, 256, C.byref(n))
+        for a, b in zip(ids[:n.value], ms[:n.value]):
+            prof.setdefault(int(a), []).append(float(b))
+        nvis = max(nvis, s.map().GetNumVisibleBlocks())
+    nprof = max(args.profile_frames, 1)
+    per_frame = {k: sum(v) / nprof for k, v in prof.items()}
+    per_launch = {k: sum(v) / len(v) for k, v in prof.items()}
+    P = [(W >> l) * (H >> l) for l in range(3)]
+    # dominant kernel among those with an algorithmic byte count
+    cands = {k: per_frame[k] for k in per_frame if not np.isnan(stage_bytes(k, P, nvis, 4, P[0]))}
+    dom = max(cands, key=cands.get)
+    dom_bytes = stage_bytes(dom, P, nvis, 4, P[0])
+    achieved = dom_bytes / (per_launch[dom] * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(stage_name(dom))
+        except Exception:
+            traffic = None
+
+    # ---------------- e2e through the C ABI with host buffers
+    s2 = new_session()
+    pin_rgb = [torch.from_numpy(f.rgb).pin_memory().numpy() for f in frames[:nframes]]
+    pin_dep = [torch.from_numpy(f.depth.view(np.int16)).pin_memory().numpy().view(np.uint16)
+               for f in frames[:nframes]]
+    s2.process(pin_rgb[0], pin_dep[0])
+    for i in range(1, 1 + args.warmup):
+        s2.process(pin_rgb[i], pin_dep[i])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(1 + args.warmup, nframes):
+        s2.process(pin_rgb[i], pin_dep[i])
+    e2e_s = time.perf_counter() - t0
+    s2.close()
+
+    # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
+    cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
+
+    value = world * args.steps / (total_ms * 1e-3)
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 compute, fp16 TSDF storage, fp64 solve",
+        "data": "synthetic (seeded analytic RGB-D scene; no dataset)",
+        "config": dict(WORKLOAD, l2="flushed between steps (256 MB write outside the timed events)",
+                       parallelism="replicas" if world > 1 else "single session",
+                       p50_ms=round(lat[len(lat) // 2], 4), p99_ms=round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
+                       frame_status_nonzero=int(sum(1 for x in statuses if x != 0)),
+                       stage_ms_per_frame={stage_name(k): round(v, 4) for k, v in sorted(per_frame.items())},
+                       visible_blocks=nvis),
+        "e2e": {"value": round(world * args.steps / e2e_s, 2), "unit": "frames/s",
+                "h2d_bytes_per_step": W * H * 3 + W * H * 2, "d2h_bytes_per_step": 256},
+        "gpu_launches": kernels * args.steps,
+        "roofline": {"bound": "hbm", "kernel": stage_name(dom), "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": round(per_launch[dom], 5),
+                     "traffic": traffic},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
+    import oracle
+
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    o = oracle.Session(W, H, K, WORKLOAD["voxel_m"], WORKLOAD["trunc_m"], levels=3, iters=(10, 5, 3), kind="f32")
+    o.frame(frames[0].rgb, frames[0].depth)
+    t0 = time.perf_counter()
+    n = 0
+    for f in frames[1:1 + nmax]:
+        o.frame(f.rgb, f.depth)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt, 3), "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n} tracked frames (after the initialising frame) of the same 640x480 5 mm sequence"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle  # noqa: F401
+    from yetanotherslam_gb300 import synth
+
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    K = synth.intrinsics(W, H)
+    warm = min(args.warmup, 2)
+    steps = min(args.steps, args.cpu_frames)
+    frames = make_frames(1 + warm + steps, W, H, WORKLOAD["scene_seed"])
+    import oracle as orc
+
+    o = orc.Session(W, H, K, WORKLOAD["voxel_m"], WORKLOAD["trunc_m"], levels=3, iters=(10, 5, 3), kind="f32")
+    o.frame(frames[0].rgb, frames[0].depth)
+    for f in frames[1:1 + warm]:
+        o.frame(f.rgb, f.depth)
+    t0 = time.perf_counter()
+    n = 0
+    for f in frames[1 + warm:]:
+        o.frame(f.rgb, f.depth)
+        n += 1
+        if time.perf_counter() - t0 > 150.0:
+            break
+    dt = time.perf_counter() - t0
+    v = round(n / dt, 3)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 0,
+        "steps": n, "warmup": warm, "ms_per_step": round(1e3 * dt / max(n, 1), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": dict(WORKLOAD, note="CPU restatement of the reference's dense path (the reference needs OpenCV "
+                                      "CUDA, Eigen, Sophus and does not build here); FP32, OpenMP"),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{n} tracked frames of the 640x480 5 mm sequence"},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="yas", choices=["yas", "reference"])
+    ap.add_argument("--profile-frames", type=int, default=4)
+    ap.add_argument("--cpu-frames", type=int, default=8)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

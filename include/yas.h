@@ -1,0 +1,283 @@
+/*
+ * yas.h — C ABI of the GB300-native dense RGB-D path (voxel-hash TSDF fusion,
+ * raycasting, marching cubes, dense ICP + photometric tracking).
+ *
+ * Every entry point is a plain C function over opaque handles, POD structs,
+ * raw pointers and sizes.  Every call returns an int status (YAS_OK == 0).
+ * Each handle owns one CUDA stream (`stream` at creation; NULL = the legacy
+ * default stream) and every device operation of that handle is ordered on it.
+ *
+ * The handles mirror the classes of YetAnotherSLAM's RGBDFusion library; each
+ * declaration cites the reference member it replaces (paths relative to the
+ * reference project root).
+ *
+ * Pose convention: yas_pose is a row-major 3x4 [R|t] in double precision.
+ * `Tcm` maps camera coordinates to map (submap) coordinates, as the
+ * reference's Sophus::SE3d Tcm argument of MapStruct::Fuse / RayTrace.
+ */
+#ifndef YAS_H
+#define YAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define YAS_API __attribute__((visibility("default")))
+#else
+#define YAS_API
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum yas_status {
+    YAS_OK = 0,
+    YAS_ERR_BAD_ARG = 1,       /* null handle / bad size / bad enum          */
+    YAS_ERR_OOM = 2,           /* device or pinned-host allocation failed    */
+    YAS_ERR_CUDA = 3,          /* a CUDA runtime call failed                 */
+    YAS_ERR_TABLE_FULL = 4,    /* hash probe limit reached on insert         */
+    YAS_ERR_POOL_FULL = 5,     /* voxel-block pool exhausted                 */
+    YAS_ERR_NUMERIC = 6,       /* NaN in the Gauss-Newton solve              */
+    YAS_ERR_TRACK_LOST = 7,    /* |translation| of the frame step > limit    */
+    YAS_ERR_MESH_OVERFLOW = 8, /* more triangles than the mesher's capacity  */
+    YAS_ERR_STATE = 9,         /* call not valid in the handle's state       */
+    YAS_ERR_COORD_RANGE = 10,  /* block coordinate outside the 21-bit range  */
+    YAS_ERR_CAPACITY = 11      /* caller buffer too small                    */
+};
+
+/* Human-readable name of a status code (static string). */
+YAS_API const char *yas_status_string(int status);
+/* Library version string, e.g. "yas-gb300 0.1.0 sm_103a". */
+YAS_API const char *yas_version(void);
+
+/* ---------------------------------------------------------------- PODs */
+typedef struct yas_intrinsics {
+    float fx, fy, cx, cy;
+} yas_intrinsics;
+
+typedef struct yas_pose {
+    double m[12]; /* row-major [R | t] */
+} yas_pose;
+
+/* TSDF voxel storage formats.  All formats keep the reference's update rule
+ * (running weighted average, weight + 1 capped at 255). */
+enum yas_voxel_format {
+    YAS_VOXEL_F32 = 0, /* float sdf + float weight, 8 B/voxel              */
+    YAS_VOXEL_F16 = 1, /* fp16 sdf + u16 weight, 4 B/voxel                 */
+    YAS_VOXEL_S24 = 2  /* 24-bit fixed-point sdf (2^-22 step) + u8 weight, 4 B */
+};
+
+typedef struct yas_map_config {
+    int hash_slots;    /* open-addressing slots, power of two               */
+    int max_blocks;    /* voxel-block pool capacity (8^3 voxels per block)  */
+    float voxel_size;  /* metres                                            */
+    float trunc_dist;  /* metres                                            */
+    float depth_min;   /* fusion/visibility gate; reference: 0.1 m          */
+    float depth_max;   /* fusion/visibility gate; reference: 3.0 m          */
+    int voxel_format;  /* enum yas_voxel_format                             */
+    int max_weight;    /* weight cap; reference: 255                        */
+} yas_map_config;
+
+/* Fills `cfg` with the reference's constants (depth 0.1..3.0 m, weight cap
+ * 255) for the given grid; VoxelMap.cu:812-813,852-853. */
+YAS_API int yas_map_config_default(yas_map_config *cfg, int hash_slots, int max_blocks,
+                                   float voxel_size, float trunc_dist, int voxel_format);
+
+/* ---------------------------------------------------------------- MapStruct
+ * Replaces class MapStruct (RGBDFusion/include/VoxelMap.h:32-144). */
+typedef struct yas_map yas_map;
+
+/* MapStruct(K) + create(...) + Reset(): VoxelMap.h:35,38,45; VoxelMap.cu:46-93. */
+YAS_API int yas_map_create(yas_map **out, const yas_map_config *cfg, const yas_intrinsics *K,
+                           void *stream);
+/* MapStruct::create(hashTableSize, bucketSize, voxelBlockSize, voxelSize,
+ * truncationDist) argument form, VoxelMap.h:35 / VoxelMap.cu:60-81.  The slot
+ * count becomes the power of two >= max(hashTableSize, 2*voxelBlockSize). */
+YAS_API int yas_map_create_ref(yas_map **out, int hashTableSize, int bucketSize, int voxelBlockSize,
+                               float voxelSize, float truncationDist, const yas_intrinsics *K,
+                               void *stream);
+/* MapStruct::Release(): VoxelMap.h:48 / VoxelMap.cu:104-136 (also frees the handle). */
+YAS_API int yas_map_destroy(yas_map *map);
+/* MapStruct::Reset(): VoxelMap.h:45 / VoxelMap.cu:46-58. */
+YAS_API int yas_map_reset(yas_map *map);
+/* MapStruct::Empty(): VoxelMap.h:46 / VoxelMap.cu:138-141 (no allocated block). */
+YAS_API int yas_map_empty(yas_map *map, int *out_empty);
+/* MapStruct::Fuse(GpuMat depth, SE3d Tcm): VoxelMap.h:61 / VoxelMap.cu:825-884.
+ * depth: float metres, `on_device` = 1 for a device pointer, 0 for host. */
+YAS_API int yas_map_fuse_depth(yas_map *map, const float *depth, int width, int height,
+                               int pitch_bytes, int on_device, const yas_pose *Tcm);
+/* MapStruct::CheckNumVisibleBlocks(cols, rows, Tcm): VoxelMap.h:59 / VoxelMap.cu:788-823. */
+YAS_API int yas_map_check_visible(yas_map *map, int cols, int rows, const yas_pose *Tcm,
+                                  unsigned *out_count);
+/* MapStruct::GetNumVisibleBlocks(): VoxelMap.h:58 / VoxelMap.cu:201-206. */
+YAS_API int yas_map_num_visible(yas_map *map, unsigned *out_count);
+/* Number of allocated blocks (no reference counterpart; heap pointer). */
+YAS_API int yas_map_num_allocated(yas_map *map, unsigned *out_count);
+/* Sticky device error bits of the map (YAS_ERR_* as 1<<code), cleared on read. */
+YAS_API int yas_map_take_errors(yas_map *map, unsigned *out_bits);
+/* Copies every allocated block to host arrays: coords[3*i] = block x,y,z,
+ * sdf/weight[512*i + z*64 + y*8 + x] (float).  Order: pool order. */
+YAS_API int yas_map_export(yas_map *map, int *coords, float *sdf, float *weight, unsigned capacity,
+                           unsigned *out_count);
+/* Inserts blocks with given contents (the inverse of yas_map_export). */
+YAS_API int yas_map_import(yas_map *map, const int *coords, const float *sdf, const float *weight,
+                           unsigned count);
+/* MapStruct::visibleTable contents as block coords (host), VoxelMap.h:127-128. */
+YAS_API int yas_map_export_visible(yas_map *map, int *coords, unsigned capacity, unsigned *out_count);
+/* MapStruct::GetPose / SetPose (host-side mTcw), VoxelMap.h:40-41 / VoxelMap.cu:12-22. */
+YAS_API int yas_map_get_pose(yas_map *map, yas_pose *out);
+YAS_API int yas_map_set_pose(yas_map *map, const yas_pose *Tcw);
+/* MapStruct::SetActiveFlag / isActive, VoxelMap.h:73-74 / VoxelMap.cu:989-999. */
+YAS_API int yas_map_set_active(yas_map *map, int flag);
+YAS_API int yas_map_is_active(yas_map *map, int *out);
+/* MapStruct::Hibernate / ReActivate (host swap of all device arrays),
+ * VoxelMap.h:69-71 / VoxelMap.cu:894-954. */
+YAS_API int yas_map_hibernate(yas_map *map);
+YAS_API int yas_map_reactivate(yas_map *map);
+YAS_API int yas_map_is_hibernated(yas_map *map, int *out);
+/* Device-memory footprint in bytes (tables, pool, lists). */
+YAS_API int yas_map_device_bytes(yas_map *map, size_t *out_bytes);
+
+/* ---------------------------------------------------------------- RayTraceEngine
+ * Replaces class RayTraceEngine (RGBDFusion/include/RayTraceEngine.h:11-49). */
+typedef struct yas_raycaster yas_raycaster;
+
+/* RayTraceEngine(w, h, K): RayTraceEngine.h:15 / RayTraceEngine.cu:11-29. */
+YAS_API int yas_raycaster_create(yas_raycaster **out, int width, int height,
+                                 const yas_intrinsics *K, void *stream);
+YAS_API int yas_raycaster_destroy(yas_raycaster *rc);
+/* RayTraceEngine::RayTrace(MapStruct*, Tcm): RayTraceEngine.h:16 / RayTraceEngine.cu:412-450. */
+YAS_API int yas_raycaster_raycast(yas_raycaster *rc, yas_map *map, const yas_pose *Tcm);
+/* RayTraceEngine::GetVMap(): device float4 vertex map (camera frame, w=+1 hit,
+ * w=-1 miss), row pitch in bytes. RayTraceEngine.h:27 / RayTraceEngine.cu:452-455. */
+YAS_API int yas_raycaster_vmap(yas_raycaster *rc, const float **dev_vmap, int *pitch_bytes);
+/* MapStruct::GetRayTracingResultDepth(): VMapToDepth of the last raycast into
+ * `depth` (float metres, 0 = miss), VoxelMap.cu:981-987 / ImageProc.cu:262-286. */
+YAS_API int yas_raycaster_depth(yas_raycaster *rc, float *depth, int pitch_bytes, int on_device);
+/* RayTraceEngine::GetNumVisibleBlock / GetNumRenderingBlocks: RayTraceEngine.h:25-26. */
+YAS_API int yas_raycaster_num_visible(yas_raycaster *rc, unsigned *out);
+YAS_API int yas_raycaster_num_rendering_blocks(yas_raycaster *rc, unsigned *out);
+/* Copies the (W/8)x(H/8) z-range maps (near, far) to host float arrays. */
+YAS_API int yas_raycaster_zrange(yas_raycaster *rc, float *znear, float *zfar);
+
+/* ---------------------------------------------------------------- MeshEngine
+ * Replaces class MeshEngine (RGBDFusion/include/MeshEngine.h:8-24). */
+typedef struct yas_mesher yas_mesher;
+
+/* MeshEngine(MaxNumTriangle): MeshEngine.h:12 / MeshEngine.cu:271-277. */
+YAS_API int yas_mesher_create(yas_mesher **out, int max_triangles, void *stream);
+YAS_API int yas_mesher_destroy(yas_mesher *me);
+/* MeshEngine::Meshify(MapStruct*) device part: MeshEngine.h:13 / MeshEngine.cu:293-331.
+ * Triangles are emitted block by block in pool order (deterministic for a given map). */
+YAS_API int yas_mesher_meshify(yas_mesher *me, yas_map *map, unsigned *out_num_triangles);
+/* D2H of the soup: 9 floats per triangle (3 vertices, submap metres) and the
+ * face normal repeated per vertex, as MapStruct::mplPoint / mplNormal (N = 9 * count),
+ * MeshEngine.cu:332-339. */
+YAS_API int yas_mesher_copy(yas_mesher *me, float *points, float *normals, unsigned capacity_tris);
+/* Per-triangle marching-cubes case index and global voxel position (for
+ * topology checks): cases[i], cube_xyz[3*i]. */
+YAS_API int yas_mesher_copy_cases(yas_mesher *me, int *cases, int *cube_xyz, unsigned capacity_tris);
+
+/* ---------------------------------------------------------------- RGBDTracking
+ * Replaces class RGBDTracking (RGBDFusion/include/RGBDTracking.h:9-107). */
+typedef struct yas_tracker yas_tracker;
+
+enum yas_track_mode { YAS_TRACK_RGB = 1, YAS_TRACK_ICP = 2, YAS_TRACK_RGBD = 3 };
+
+/* RGBDTracking(w, h, K, bRGB, bIcp): RGBDTracking.h:13 / RGBDTracking.cu:5-64.
+ * K: row-major 3x3 double.  num_levels <= 5 (reference: 5); iterations[l] is
+ * the GN iteration count at level l (reference: {10,5,3,3,3}). */
+YAS_API int yas_tracker_create(yas_tracker **out, int width, int height, const double *K,
+                               int num_levels, const int *iterations, int mode, void *stream);
+YAS_API int yas_tracker_destroy(yas_tracker *tr);
+/* SetReferenceImage / SetTrackingImage (CV_8U gray): RGBDTracking.h:17,20 / .cu:66-116. */
+YAS_API int yas_tracker_set_reference_image(yas_tracker *tr, const uint8_t *gray, int pitch_bytes,
+                                            int on_device);
+YAS_API int yas_tracker_set_tracking_image(yas_tracker *tr, const uint8_t *gray, int pitch_bytes,
+                                           int on_device);
+/* SetReferenceDepth / SetTrackingDepth (CV_32F metres): RGBDTracking.h:18,21 / .cu:80-138. */
+YAS_API int yas_tracker_set_reference_depth(yas_tracker *tr, const float *depth, int pitch_bytes,
+                                            int on_device);
+YAS_API int yas_tracker_set_tracking_depth(yas_tracker *tr, const float *depth, int pitch_bytes,
+                                           int on_device);
+/* SetReferenceModel(GpuMat vmap): RGBDTracking.h:23 / RGBDTracking.cu:140-150.
+ * vmap: device float4 (w=+1 valid). */
+YAS_API int yas_tracker_set_reference_model(yas_tracker *tr, const float *dev_vmap, int pitch_bytes);
+/* GetTransform(init, bSwapBuffer): RGBDTracking.h:27 / RGBDTracking.cu:152-214. */
+YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int swap_buffer,
+                                      yas_pose *out);
+/* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
+YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);
+YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);
+/* One Gauss-Newton linearisation at pose T on `level` (ComputeSingleStep*,
+ * RGBDTracking.cu:225-292, 408-441, 521-545): H (36, row-major), b (6), and
+ * stats[4] = {sum r^2 used for the error, residual count, rgb sigma, icp count}. */
+YAS_API int yas_tracker_compute_step(yas_tracker *tr, int level, const yas_pose *T, double *H,
+                                     double *b, double *stats);
+/* Device pointers of pyramid level buffers (for inspection/tests).
+ * which: 0 cur intensity, 1 cur gx, 2 cur gy, 3 cur inv-depth, 4 cur vmap,
+ * 5 cur nmap, 6 ref intensity, 7 ref inv-depth, 8 ref vmap, 9 ref nmap. */
+YAS_API int yas_tracker_level_buffer(yas_tracker *tr, int level, int which, const void **dev_ptr,
+                                     int *width, int *height, int *pitch_bytes);
+
+/* ---------------------------------------------------------------- session
+ * One SLAM session: a submap, a raycaster and a tracker whose per-frame dense
+ * work (Tracking::TrackRGBD + Tracking::StereoInitialization dense calls,
+ * FullSystem/src/Tracking.cpp:139-155,162-197; System::TrackRGBD colour and
+ * depth conversion, FullSystem/src/System.cpp:43-65) runs as one captured
+ * CUDA graph with no host round trip inside the frame. */
+typedef struct yas_session yas_session;
+
+typedef struct yas_session_config {
+    int width, height;
+    yas_intrinsics K;
+    yas_map_config map;
+    int num_levels;        /* pyramid levels (<= 5)                          */
+    int iterations[5];     /* GN iterations per level, finest first          */
+    int mode;              /* enum yas_track_mode                            */
+    float depth_scale;     /* metres per depth unit (u16 mm: 0.001)          */
+    float max_step_translation; /* frame-step rejection, reference 0.1 m     */
+    int use_graph;         /* 1: capture the frame into a CUDA graph          */
+} yas_session_config;
+
+YAS_API int yas_session_config_default(yas_session_config *cfg, int width, int height,
+                                       const yas_intrinsics *K, int hash_slots, int max_blocks,
+                                       float voxel_size, float trunc_dist, int voxel_format);
+YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg, void *stream);
+YAS_API int yas_session_destroy(yas_session *s);
+/* Enqueues one frame (RGB u8 interleaved w*h*3, depth u16 w*h) without waiting.
+ * Inputs on the host must stay valid until yas_session_wait returns; they are
+ * copied to the device on the session stream. */
+YAS_API int yas_session_submit(yas_session *s, const uint8_t *rgb, const uint16_t *depth,
+                               int on_device);
+/* Waits for the last submitted frame; returns its map pose Tcm and frame status
+ * (YAS_OK, YAS_ERR_TRACK_LOST, YAS_ERR_NUMERIC, ...). */
+YAS_API int yas_session_wait(yas_session *s, yas_pose *out_Tcm, int *out_frame_status);
+/* submit + wait. */
+YAS_API int yas_session_process_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth,
+                                      int on_device, yas_pose *out_Tcm, int *out_frame_status);
+YAS_API int yas_session_map(yas_session *s, yas_map **out);
+YAS_API int yas_session_tracker(yas_session *s, yas_tracker **out);
+YAS_API int yas_session_raycaster(yas_session *s, yas_raycaster **out);
+YAS_API int yas_session_frame_count(yas_session *s, int *out);
+/* Device pointer of the session's float depth (metres) of the last frame. */
+YAS_API int yas_session_depth(yas_session *s, const float **dev_depth, int *pitch_bytes);
+/* Number of kernels the last frame launched (graph nodes of kind kernel). */
+YAS_API int yas_session_kernels_per_frame(yas_session *s, int *out);
+
+/* Stream of a handle (cudaStream_t as void*), for event timing by callers. */
+YAS_API void *yas_session_stream(yas_session *s);
+/* Runs one tracked frame eagerly with a CUDA event before every launch group
+ * and returns the device time of each group: stage_ids[i] is 0 image
+ * pyramid, 1 depth pyramid, 2 z-range, 3 ray march, 4 model pyramid, 5 GN
+ * init, 10+l / 20+l GN pass A / B at level l, 6 frame finalize, 7 block
+ * allocation, 8 visibility, 9 integration; stage_ms[i] its duration. */
+YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device,
+                                      int *stage_ids, float *stage_ms, int capacity, int *out_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* YAS_H */

@@ -1,0 +1,193 @@
+"""Parity of the voxel-hash map against the oracle, through the C ABI.
+
+Reference behaviour: RGBDFusion/src/VoxelMap.cu:517-884 (allocation,
+visibility, integration).  Bars:
+  * allocated block coordinate set and visible set: bit-exact;
+  * voxel weights: exact (integers);
+  * TSDF (normalised by the truncation distance): F32 and S24 storage within
+    1e-5, F16 storage within 1e-3 over these short sequences (weights <= 6),
+    all against the FP64 oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.helpers import align_blocks, rel_poses, sequence
+from yetanotherslam_gb300 import rgbdfusion as rf
+from yetanotherslam_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+TOL = {rf.VOXEL_F32: 1e-5, rf.VOXEL_S24: 1e-5, rf.VOXEL_F16: 1e-3}
+
+
+def _pair(fmt, K, vs=0.008, slots=1 << 20, blocks=1 << 17):
+    m = rf.MapStruct(K)
+    m.create_config(slots, blocks, vs, 3 * vs, fmt)
+    o = oracle.Map(vs, 3 * vs)
+    return m, o
+
+
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16, rf.VOXEL_S24])
+def test_fuse_sequence_matches_oracle(cuda, fmt):
+    W, H = 640, 480
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, 6, W, H)
+    poses = rel_poses(seq)
+    m, o = _pair(fmt, K)
+    for i, (rgb, d16, dm, _) in enumerate(seq):
+        m.Fuse(dm, poses[i])
+        o.fuse(dm, K, poses[i])
+        # visible set of this fusion (MapStruct::visibleTable)
+        vg = m.visible_coords()
+        vo = o.visible(W, H, K, poses[i])
+        assert {tuple(r) for r in vg} == {tuple(r) for r in vo}, f"frame {i}: visible sets differ"
+        assert len(vg) == len(vo)
+    assert m.take_errors() == 0
+    cg, sg, wg = m.export()
+    co, so, wo = o.export()
+    sg, wg, so, wo = align_blocks(cg, sg, wg, co, so, wo)
+    assert np.array_equal(wg, wo), "weights differ"
+    obs = wo > 0
+    err = np.abs(sg[obs] - so[obs])
+    assert obs.sum() > 100000
+    assert err.max() <= TOL[fmt], f"max TSDF error {err.max():.3g} (p99.9 {np.quantile(err, 0.999):.3g})"
+
+
+def test_allocation_only_bit_exact_various_poses(cuda):
+    """Allocation from a depth map at poses with arbitrary rotations."""
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    seq = sequence(5, 3, W, H)
+    rng = np.random.default_rng(0)
+    m, o = _pair(rf.VOXEL_F32, K, vs=0.005)
+    for k in range(4):
+        a = rng.normal(size=3)
+        a = a / np.linalg.norm(a) * rng.uniform(0, np.pi)
+        th = np.linalg.norm(a)
+        Wx = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]]) / th
+        T = np.eye(4)
+        T[:3, :3] = np.eye(3) + np.sin(th) * Wx + (1 - np.cos(th)) * Wx @ Wx
+        T[:3, 3] = rng.uniform(-3, 3, size=3)
+        dm = seq[k % 3][2]
+        m.Fuse(dm, T)
+        o.fuse(dm, K, T)
+    cg, sg, wg = m.export()
+    co, so, wo = o.export()
+    sg, wg, so, wo = align_blocks(cg, sg, wg, co, so, wo)
+    assert np.array_equal(wg, wo)
+    assert np.abs(sg - so)[wo > 0].max() <= TOL[rf.VOXEL_F32]
+
+
+def test_empty_nan_and_out_of_range_depth(cuda):
+    W, H = 64, 48
+    K = synth.intrinsics(W, H)
+    m, o = _pair(rf.VOXEL_F16, K)
+    for d in (np.zeros((H, W), np.float32), np.full((H, W), np.nan, np.float32),
+              np.full((H, W), 5.0, np.float32), np.full((H, W), 0.05, np.float32)):
+        m.Fuse(d, np.eye(4))
+        o.fuse(d, K, np.eye(4))
+    assert m.num_allocated() == 0 == o.num_blocks
+    assert m.Empty()
+    assert m.take_errors() == 0
+
+
+def test_tiny_and_ragged_images(cuda):
+    for W, H in [(1, 1), (7, 5), (33, 17)]:
+        K = (30.0, 30.0, (W - 1) / 2, (H - 1) / 2)
+        d = np.full((H, W), 1.2, np.float32)
+        d[::2, ::3] = 0.7
+        m, o = _pair(rf.VOXEL_F32, K, vs=0.004)
+        m.Fuse(d, np.eye(4))
+        o.fuse(d, K, np.eye(4))
+        cg, sg, wg = m.export()
+        co, so, wo = o.export()
+        sg, wg, so, wo = align_blocks(cg, sg, wg, co, so, wo)
+        assert np.array_equal(wg, wo)
+
+
+def test_device_and_host_inputs_agree(cuda):
+    import torch
+
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    dm = sequence(3, 1, W, H)[0][2]
+    a, _ = _pair(rf.VOXEL_F16, K)
+    b, _ = _pair(rf.VOXEL_F16, K)
+    a.Fuse(dm, np.eye(4))
+    b.Fuse(torch.from_numpy(dm).cuda(), np.eye(4))
+    torch.cuda.synchronize()
+    ca, sa, wa = a.export()
+    cb, sb, wb = b.export()
+    sa, wa, sb, wb = align_blocks(ca, sa, wa, cb, sb, wb)
+    assert np.array_equal(sa, sb) and np.array_equal(wa, wb)
+
+
+def test_pool_exhaustion_reports_error(cuda):
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    dm = sequence(3, 1, W, H)[0][2]
+    m = rf.MapStruct(K)
+    m.create_config(1 << 16, 64, 0.008, 0.024, rf.VOXEL_F16)
+    m.Fuse(dm, np.eye(4))
+    assert m.num_allocated() == 64
+    bits = m.take_errors()
+    assert bits & (1 << 5), "POOL_FULL not reported"
+    assert m.take_errors() == 0  # cleared on read
+
+
+def test_table_full_reports_error(cuda):
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    dm = sequence(3, 1, W, H)[0][2]
+    m = rf.MapStruct(K)
+    m.create_config(64, 1 << 14, 0.008, 0.024, rf.VOXEL_F16)
+    m.Fuse(dm, np.eye(4))
+    assert m.num_allocated() == 64
+    assert m.take_errors() & (1 << 4), "TABLE_FULL not reported"
+
+
+def test_export_import_and_hibernate_roundtrip(cuda):
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, 2, W, H)
+    poses = rel_poses(seq)
+    m, _ = _pair(rf.VOXEL_S24, K)
+    for i in range(2):
+        m.Fuse(seq[i][2], poses[i])
+    c0, s0, w0 = m.export()
+    m.Hibernate()
+    assert m.mbInHibernation
+    m.ReActivate()
+    c1, s1, w1 = m.export()
+    assert np.array_equal(c0, c1) and np.array_equal(s0, s1) and np.array_equal(w0, w1)
+    n = rf.MapStruct(K)
+    n.create_config(1 << 16, 1 << 15, 0.008, 0.024, rf.VOXEL_S24)
+    n.import_blocks(c0, s0, w0)
+    c2, s2, w2 = n.export()
+    s0a, w0a, s2a, w2a = align_blocks(c0, s0, w0, c2, s2, w2)
+    assert np.array_equal(s0a, s2a) and np.array_equal(w0a, w2a)
+    # fusing continues identically after a hibernate/reactivate cycle
+    m.Fuse(seq[1][2], poses[1])
+    n.Fuse(seq[1][2], poses[1])
+    ca, sa, wa = m.export()
+    cb, sb, wb = n.export()
+    sa, wa, sb, wb = align_blocks(ca, sa, wa, cb, sb, wb)
+    assert np.array_equal(sa, sb) and np.array_equal(wa, wb)
+
+
+def test_reset_clears_map(cuda):
+    W, H = 160, 120
+    K = synth.intrinsics(W, H)
+    dm = sequence(3, 1, W, H)[0][2]
+    m, _ = _pair(rf.VOXEL_F32, K)
+    m.Fuse(dm, np.eye(4))
+    assert m.num_allocated() > 0
+    m.Reset()
+    assert m.num_allocated() == 0 and m.Empty()
+    m.Fuse(dm, np.eye(4))
+    o = oracle.Map(0.008, 0.024)
+    o.fuse(dm, K, np.eye(4))
+    assert m.num_allocated() == o.num_blocks

@@ -1,0 +1,119 @@
+"""Dense tracker parity against the oracle, through the C ABI.
+
+Reference behaviour: RGBDFusion/src/RGBDTracking.cu:66-545 and
+RGBDFusion/include/TrackingUtils.h.  Bars:
+  * pyramids: inverse depth bit-exact, intensity/gradients within 1e-3
+    (grey levels), vertex maps within 1e-5 m, normal validity identical on
+    99.99 % of pixels;
+  * one Gauss-Newton linearisation from the same pose: every entry of H and
+    b within 1e-3 of max|H| (resp. max|b|);
+  * GetTransform: pose within 1e-4 m and 1e-4 rad of the oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.helpers import pose_error, rel_poses, sequence
+from yetanotherslam_gb300 import rgbdfusion as rf
+from yetanotherslam_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _K33(W, H):
+    fx, fy, cx, cy = synth.intrinsics(W, H)
+    return np.array([[fx, 0, cx], [0, fy, cy], [0, 0, 1.0]])
+
+
+def _setup(mode, W=320, H=240, levels=3, iters=(10, 5, 3)):
+    K = _K33(W, H)
+    seq = sequence(11, 2, W, H)
+    poses = rel_poses(seq)
+    g0, g1 = synth.gray_of(seq[0][0]), synth.gray_of(seq[1][0])
+    d0, d1 = seq[0][2], seq[1][2]
+    tr = rf.RGBDTracking(W, H, K, bRGB=bool(mode & 1), bIcp=bool(mode & 2), num_levels=levels, iterations=iters)
+    ot = oracle.Tracker(W, H, K, levels=levels, iters=iters, mode=mode)
+    # reference model: raycast of the map fused from frame 0 at frame 0's pose
+    m = rf.MapStruct(K)
+    m.create_config(1 << 18, 1 << 15, 0.008, 0.024, rf.VOXEL_F32)
+    m.Fuse(d0, np.eye(4))
+    rc = rf.RayTraceEngine(W, H, K)
+    rc.RayTrace(m, np.eye(4))
+    vm = rc.GetVMap()
+    for obj in (tr,):
+        obj.SetReferenceImage(g0)
+        obj.SetReferenceDepth(d0)
+        obj.SetTrackingImage(g1)
+        obj.SetTrackingDepth(d1)
+        obj.SetReferenceModel(vm)
+    ot.set_image(g0, True)
+    ot.set_depth(d0, True)
+    ot.set_image(g1, False)
+    ot.set_depth(d1, False)
+    ot.set_model(vm.numpy())
+    gt = np.linalg.inv(poses[1])  # T_cur_ref = (T_ref_cur)^-1 with the reference at the map origin
+    return tr, ot, gt
+
+
+def test_pyramids_match_oracle(cuda):
+    tr, ot, _ = _setup(3)
+    for lvl in range(3):
+        for which in range(10):
+            g = tr.level_buffer(lvl, which).numpy()
+            o = ot.level(lvl, which)
+            if which in (3, 7):
+                assert np.array_equal(g, o), f"inverse depth level {lvl} ({which})"
+            elif which in (0, 1, 2, 6):
+                assert np.abs(g - o).max() <= 1e-3, f"intensity/gradient level {lvl} ({which})"
+            elif which in (4, 8):
+                vg, vo = g[..., 3] > 0, o[..., 3] > 0
+                assert np.array_equal(vg, vo), f"vertex validity level {lvl} ({which})"
+                assert np.abs(g[vg][:, :3] - o[vo][:, :3]).max() <= 1e-5
+            else:
+                vg, vo = g[..., 3] > 0, o[..., 3] > 0
+                assert (vg == vo).mean() >= 0.9999, f"normal validity level {lvl} ({which})"
+                both = vg & vo
+                assert np.quantile(np.abs(g[both][:, :3] - o[both][:, :3]), 0.999) <= 1e-3
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_single_gauss_newton_step_matches_oracle(cuda, mode):
+    tr, ot, gt = _setup(mode)
+    perturb = np.eye(4)
+    perturb[:3, 3] = [0.004, -0.002, 0.003]
+    for lvl in range(3):
+        for T in (np.eye(4), gt, perturb @ gt):
+            Hg, bg, sg = tr.compute_step(lvl, T)
+            Ho, bo, so = ot.compute_step(lvl, T)
+            assert np.abs(Hg - Ho).max() <= 1e-3 * np.abs(Ho).max(), (lvl, np.abs(Hg - Ho).max(), np.abs(Ho).max())
+            assert np.abs(bg - bo).max() <= 1e-3 * max(np.abs(bo).max(), 1e-9), (lvl, bg, bo)
+            assert abs(sg[1] - so[1]) <= max(2, 1e-3 * so[1])  # residual count
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_get_transform_matches_oracle(cuda, mode):
+    tr, ot, gt = _setup(mode)
+    Tg = tr.GetTransform(np.eye(4), False)
+    st, To = ot.get_transform(np.eye(4), False)
+    assert st == 0 and tr.IsTrackingGood()
+    dt, dr = pose_error(To, Tg)
+    assert dt <= 1e-4 and dr <= 1e-4, (dt, dr)
+    # and both land near the true motion
+    et, er = pose_error(gt, Tg)
+    assert et < 0.01 and er < 0.01
+
+
+def test_tracking_from_no_data_returns_identity(cuda):
+    W, H = 64, 48
+    K = _K33(W, H)
+    tr = rf.RGBDTracking(W, H, K, num_levels=2, iterations=(3, 2))
+    z = np.zeros((H, W), np.float32)
+    g = np.zeros((H, W), np.uint8)
+    tr.SetReferenceImage(g)
+    tr.SetReferenceDepth(z)
+    tr.SetTrackingImage(g)
+    tr.SetTrackingDepth(z)
+    T = tr.GetTransform(np.eye(4), True)
+    assert np.allclose(T, np.eye(4))

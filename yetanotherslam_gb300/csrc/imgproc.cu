@@ -1,0 +1,233 @@
+// imgproc.cu — per-level image preprocessing for the dense tracker.
+//
+// Reference semantics (paths relative to the reference project root):
+//   RGB -> gray            FullSystem/src/System.cpp:47-49 (cv::cvtColor RGB2GRAY): BT.601
+//                          luma in 14-bit fixed point, gray = (4899 R + 9617 G + 1868 B
+//                          + 8192) >> 14 (0.299/0.587/0.114 scaled by 2^14 and rounded).
+//   u16 -> metres          System.cpp:52 (convertTo with the depth scale).
+//   intensity pyramid      RGBDTracking.cu:66-116 (cv::cuda::pyrDown: separable
+//                          [1 4 6 4 1]/16 Gaussian, reflect-101 border, keep even samples).
+//   gradients              ImageProc.cu:7-40: 0.5 * central difference, 0 on the border.
+//   inverse depth          ImageProc.cu:141-164: 1/z for 0.2 < z < 8, else 0.
+//   nearest pyr-down       ImageProc.cu:166-187: dst(x,y) = src(2x,2y); the reference
+//                          leaves the last row and column unwritten, here they are
+//                          written as invalid (0 / w = -1).
+//   vertex map             ImageProc.cu:189-220: z = 1/invz, valid when invz > 0 and z < 3.
+//   normal map             ImageProc.cu:222-260: normalize((v(x,y+1)-v)x(v(x+1,y)-v)),
+//                          invalid on the last row/column or when a vertex is invalid.
+//   model pyramid          RGBDTracking.cu:140-150 (SetReferenceModel); the reference runs
+//                          the float pyr-down on the float4 model (its coarse model levels
+//                          are unusable); here the intended float4 nearest pyr-down is used.
+#include "yas_internal.h"
+#include "yas_track.h"
+
+namespace yas {
+
+__device__ __forceinline__ float gray_of(const uint8_t *p, int channels, int bgr) {
+    if (channels == 1) return (float)p[0];
+    int r = bgr ? p[2] : p[0];
+    int g = p[1];
+    int b = bgr ? p[0] : p[2];
+    return (float)((r * 4899 + g * 9617 + b * 1868 + 8192) >> 14);
+}
+
+// Level 0 intensity (+ gradients) from gray u8 or interleaved RGB u8.
+__global__ void image_level0_kernel(const uint8_t *__restrict__ src, int channels, int bgr, int pitch,
+                                    int w, int h, float *inten, float *gx, float *gy) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const uint8_t *row = src + (size_t)y * pitch;
+    const float c = gray_of(row + x * channels, channels, bgr);
+    inten[y * w + x] = c;
+    if (x < 1 || y < 1 || x > w - 2 || y > h - 2) {
+        gx[y * w + x] = 0.0f;
+        gy[y * w + x] = 0.0f;
+    } else {
+        float l = gray_of(row + (x - 1) * channels, channels, bgr);
+        float r = gray_of(row + (x + 1) * channels, channels, bgr);
+        float u = gray_of(src + (size_t)(y - 1) * pitch + x * channels, channels, bgr);
+        float d = gray_of(src + (size_t)(y + 1) * pitch + x * channels, channels, bgr);
+        gx[y * w + x] = (r - l) * 0.5f;
+        gy[y * w + x] = (d - u) * 0.5f;
+    }
+}
+
+__device__ __forceinline__ int reflect101(int i, int n) {
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+    return i;
+}
+
+// Gaussian pyr-down of a float image: vertical 5-tap pass then horizontal.
+__global__ void pyrdown_kernel(const float *__restrict__ src, int sw, int sh, float *dst, int dw, int dh) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dw || y >= dh) return;
+    const float k[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+    int rows[5], cols[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        rows[i] = reflect101(2 * y + i - 2, sh);
+        cols[i] = reflect101(2 * x + i - 2, sw);
+    }
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        float col = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) col += k[i] * __ldg(src + (size_t)rows[i] * sw + cols[j]);
+        acc += k[j] * col;
+    }
+    dst[y * dw + x] = acc;
+}
+
+__global__ void gradient_kernel(const float *__restrict__ src, int w, int h, float *gx, float *gy) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    if (x < 1 || y < 1 || x > w - 2 || y > h - 2) {
+        gx[y * w + x] = 0.0f;
+        gy[y * w + x] = 0.0f;
+    } else {
+        gx[y * w + x] = (src[y * w + x + 1] - src[y * w + x - 1]) * 0.5f;
+        gy[y * w + x] = (src[(y + 1) * w + x] - src[(y - 1) * w + x]) * 0.5f;
+    }
+}
+
+__device__ __forceinline__ float inv_depth_of(float z) {
+    return (z > 0.2f && z < 8.0f) ? 1.0f / z : 0.0f;
+}
+
+__device__ __forceinline__ float4 vertex_of(float invz, int x, int y, const LevelCam &c) {
+    float z = 1.0f / invz;
+    if (invz > 0.0f && z < 3.0f)
+        return make_float4(z * ((float)x - c.cx) * c.invfx, z * ((float)y - c.cy) * c.invfy, z, 1.0f);
+    return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+}
+
+__device__ __forceinline__ float4 normal_of(float4 v00, float4 v01, float4 v10) {
+    if (v00.w > 0.0f && v01.w > 0.0f && v10.w > 0.0f) {
+        float ax = v10.x - v00.x, ay = v10.y - v00.y, az = v10.z - v00.z;
+        float bx = v01.x - v00.x, by = v01.y - v00.y, bz = v01.z - v00.z;
+        float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+        float nn = nx * nx + ny * ny + nz * nz;
+        if (nn > 0.0f) {
+            float inv = 1.0f / sqrtf(nn);
+            nx *= inv;
+            ny *= inv;
+            nz *= inv;
+        }
+        return make_float4(nx, ny, nz, 1.0f);
+    }
+    return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+}
+
+// Raw depth value at level 0 in metres (u16 * scale, or float).
+__device__ __forceinline__ float raw_depth(const void *src, int is_u16, int pitch, float scale, int x, int y) {
+    if (is_u16) return (float)reinterpret_cast<const uint16_t *>(static_cast<const char *>(src) + (size_t)y * pitch)[x] * scale;
+    return reinterpret_cast<const float *>(static_cast<const char *>(src) + (size_t)y * pitch)[x];
+}
+
+// Level 0 depth: metres (optional), inverse depth, vertex and normal maps.
+__global__ void depth_level0_kernel(const void *__restrict__ src, int is_u16, int pitch, float scale,
+                                    LevelCam c, float *depth_m, float *invd, float4 *vmap, float4 *nmap) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= c.w || y >= c.h) return;
+    const float z = raw_depth(src, is_u16, pitch, scale, x, y);
+    const float iz = inv_depth_of(z);
+    if (depth_m) depth_m[y * c.w + x] = z;
+    invd[y * c.w + x] = iz;
+    const float4 v00 = vertex_of(iz, x, y, c);
+    vmap[y * c.w + x] = v00;
+    float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    if (x < c.w - 1 && y < c.h - 1) {
+        float4 v01 = vertex_of(inv_depth_of(raw_depth(src, is_u16, pitch, scale, x + 1, y)), x + 1, y, c);
+        float4 v10 = vertex_of(inv_depth_of(raw_depth(src, is_u16, pitch, scale, x, y + 1)), x, y + 1, c);
+        n = normal_of(v00, v01, v10);
+    }
+    nmap[y * c.w + x] = n;
+}
+
+// Inverse depth of level l at (x,y) from level l-1 (nearest, last row/col invalid).
+__device__ __forceinline__ float invd_down(const float *prev, int pw, int x, int y, int w, int h) {
+    if (x >= w - 1 || y >= h - 1) return 0.0f;
+    return __ldg(prev + (size_t)(2 * y) * pw + 2 * x);
+}
+
+__global__ void depth_pyr_kernel(const float *__restrict__ prev, int pw, LevelCam c, float *invd,
+                                 float4 *vmap, float4 *nmap) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= c.w || y >= c.h) return;
+    const float iz = invd_down(prev, pw, x, y, c.w, c.h);
+    invd[y * c.w + x] = iz;
+    const float4 v00 = vertex_of(iz, x, y, c);
+    vmap[y * c.w + x] = v00;
+    float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    if (x < c.w - 1 && y < c.h - 1) {
+        float4 v01 = vertex_of(invd_down(prev, pw, x + 1, y, c.w, c.h), x + 1, y, c);
+        float4 v10 = vertex_of(invd_down(prev, pw, x, y + 1, c.w, c.h), x, y + 1, c);
+        n = normal_of(v00, v01, v10);
+    }
+    nmap[y * c.w + x] = n;
+}
+
+// Model level 0 normals (vmap given) or level l >= 1 vmap + normals from l-1.
+__device__ __forceinline__ float4 vmap_down(const float4 *prev, int pw, int x, int y, int w, int h) {
+    if (x >= w - 1 || y >= h - 1) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    return prev[(size_t)(2 * y) * pw + 2 * x];
+}
+
+__global__ void model_level_kernel(const float4 *__restrict__ prev, int pw, int w, int h, float4 *vmap,
+                                   float4 *nmap) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float4 v00, v01, v10;
+    if (prev == nullptr) {  // level 0: vmap already in place
+        v00 = vmap[y * w + x];
+        v01 = x < w - 1 ? vmap[y * w + x + 1] : make_float4(0, 0, 0, -1);
+        v10 = y < h - 1 ? vmap[(y + 1) * w + x] : make_float4(0, 0, 0, -1);
+    } else {
+        v00 = vmap_down(prev, pw, x, y, w, h);
+        v01 = vmap_down(prev, pw, x + 1, y, w, h);
+        v10 = vmap_down(prev, pw, x, y + 1, w, h);
+        vmap[y * w + x] = v00;
+    }
+    float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    if (x < w - 1 && y < h - 1) n = normal_of(v00, v01, v10);
+    nmap[y * w + x] = n;
+}
+
+static dim3 grid2(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
+
+void launch_image_level0(const uint8_t *src, int channels, int bgr, int pitch, int w, int h, float *inten,
+                         float *gx, float *gy, cudaStream_t s) {
+    image_level0_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(src, channels, bgr, pitch, w, h, inten, gx, gy);
+}
+
+void launch_image_level(const float *prev, int pw, int ph, int w, int h, float *inten, float *gx, float *gy,
+                        cudaStream_t s) {
+    pyrdown_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(prev, pw, ph, inten, w, h);
+    if (gx) gradient_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(inten, w, h, gx, gy);
+}
+
+void launch_depth_level0(const void *src, int is_u16, int pitch, float scale, const LevelCam &c,
+                         float *depth_m, float *invd, float4 *vmap, float4 *nmap, cudaStream_t s) {
+    depth_level0_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(src, is_u16, pitch, scale, c, depth_m, invd,
+                                                                 vmap, nmap);
+}
+
+void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float4 *vmap,
+                        float4 *nmap, cudaStream_t s) {
+    depth_pyr_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(prev, pw, c, invd, vmap, nmap);
+}
+
+void launch_model_level(const float4 *prev, int pw, int w, int h, float4 *vmap, float4 *nmap,
+                        cudaStream_t s) {
+    model_level_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(prev, pw, w, h, vmap, nmap);
+}
+
+}  // namespace yas

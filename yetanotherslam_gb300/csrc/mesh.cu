@@ -1,0 +1,435 @@
+// mesh.cu — marching-cubes extraction over every allocated block.
+//
+// Reference semantics (paths relative to the reference project root):
+//   RGBDFusion/src/MeshEngine.cu:43-269 (MeshificationFunctor): a cube at voxel
+//   p uses corners p + {0,1}^3 in the order 0:(0,0,0) 1:(1,0,0) 2:(1,1,0)
+//   3:(0,1,0) 4:(0,0,1) 5:(1,0,1) 6:(1,1,1) 7:(0,1,1); all 8 must be observed
+//   (weight != 0); case bit i is set when sdf_i < 0; edge vertices use the
+//   reference's interpolation with its 1e-6 guards; positions are voxel
+//   coordinates times the voxel size (submap metres) and every triangle carries
+//   the face normal normalize((v1-v0) x (v2-v0)).
+//
+// The triangle table is not the reference's table (RGBDFusion/utils/
+// TriangleTable.h): it is generated here from cube topology.  For each case
+// the iso-contour is traced on the six faces (each face's crossings paired so
+// that inside corners stay separated on ambiguous faces), the directed face
+// segments are chained into loops, and each loop is fanned from its
+// lowest-numbered edge.  Segment direction keeps the inside (sdf < 0) region
+// on the left seen from outside the cube, which makes every triangle's normal
+// point toward the inside, the same orientation as the reference table.
+//
+// GB300 design: one CTA per block stages the 9x9x9 sdf neighbourhood in shared
+// memory (own block with 16-byte loads plus the +x/+y/+z halo from up to 7
+// neighbour blocks); pass 1 counts triangles per block, a scan assigns each
+// block a contiguous output range, pass 2 re-derives the per-thread offsets
+// and writes the soup, so the output order is a pure function of the map.
+#include <cstring>
+
+#include "yas_internal.h"
+
+namespace yas {
+
+// ---------------------------------------------------------------- tables
+constexpr int kMcMaxTriIdx = 31;  // up to 10 triangles + terminator
+
+__constant__ unsigned short c_edge_table[256];
+__constant__ signed char c_tri_table[256][kMcMaxTriIdx];
+__constant__ unsigned char c_tri_count[256];
+
+static const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+static const int kEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                 {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+static int edge_of(int a, int b) {
+    for (int e = 0; e < 12; ++e)
+        if ((kEdge[e][0] == a && kEdge[e][1] == b) || (kEdge[e][0] == b && kEdge[e][1] == a)) return e;
+    return -1;
+}
+
+// Corners of each face in counter-clockwise order about the outward normal.
+static void face_ccw(int face, int out[4]) {
+    // face: 0 x=0, 1 x=1, 2 y=0, 3 y=1, 4 z=0, 5 z=1
+    const int axis = face / 2, side = face % 2;
+    int cs[4], n = 0;
+    for (int c = 0; c < 8; ++c)
+        if (kCorner[c][axis] == side) cs[n++] = c;
+    // order the 4 corners cyclically around the face centre
+    const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+    int order[4] = {-1, -1, -1, -1};
+    for (int i = 0; i < 4; ++i) {
+        int cu = kCorner[cs[i]][u], cv = kCorner[cs[i]][v];
+        int pos = (cu == 0 && cv == 0) ? 0 : (cu == 1 && cv == 0) ? 1 : (cu == 1 && cv == 1) ? 2 : 3;
+        order[pos] = cs[i];
+    }
+    // (u, v, axis) is right-handed, so this order is CCW about +axis.
+    if (side == 1) {
+        for (int i = 0; i < 4; ++i) out[i] = order[i];
+    } else {
+        out[0] = order[0];
+        out[1] = order[3];
+        out[2] = order[2];
+        out[3] = order[1];
+    }
+}
+
+struct McTables {
+    unsigned short edge[256];
+    signed char tri[256][kMcMaxTriIdx];
+    unsigned char count[256];
+};
+
+static void build_mc_tables(McTables &t) {
+    memset(&t, 0, sizeof(t));
+    memset(t.tri, -1, sizeof(t.tri));
+    for (int c = 0; c < 256; ++c) {
+        unsigned short em = 0;
+        for (int e = 0; e < 12; ++e) {
+            bool a = (c >> kEdge[e][0]) & 1, b = (c >> kEdge[e][1]) & 1;
+            if (a != b) em |= (unsigned short)(1u << e);
+        }
+        t.edge[c] = em;
+        if (em == 0) continue;
+        int next[12];
+        for (int e = 0; e < 12; ++e) next[e] = -1;
+        for (int f = 0; f < 6; ++f) {
+            int q[4];
+            face_ccw(f, q);
+            // crossings in CCW order: edge index and kind (+1 enter inside, -1 exit)
+            int ce[4], kind[4], nc = 0;
+            for (int i = 0; i < 4; ++i) {
+                int a = q[i], b = q[(i + 1) & 3];
+                bool ia = (c >> a) & 1, ib = (c >> b) & 1;
+                if (ia != ib) {
+                    ce[nc] = edge_of(a, b);
+                    kind[nc] = ib ? +1 : -1;
+                    ++nc;
+                }
+            }
+            if (nc == 2) {
+                int ex = kind[0] < 0 ? 0 : 1;
+                next[ce[ex]] = ce[1 - ex];
+            } else if (nc == 4) {
+                // separate inside corners: each exit pairs with the previous enter
+                for (int i = 0; i < 4; ++i)
+                    if (kind[i] < 0) next[ce[i]] = ce[(i + 3) & 3];
+            }
+        }
+        int ntri = 0, w = 0;
+        bool used[12] = {false};
+        for (int start = 0; start < 12; ++start) {
+            if (!((em >> start) & 1) || used[start]) continue;
+            int loop[12], k = 0, e = start;
+            while (e >= 0 && !used[e] && k < 12) {
+                used[e] = true;
+                loop[k++] = e;
+                e = next[e];
+            }
+            // fan from the lowest edge of the loop (start is the lowest unused)
+            for (int i = 1; i + 1 < k; ++i) {
+                t.tri[c][w++] = (signed char)loop[0];
+                t.tri[c][w++] = (signed char)loop[i];
+                t.tri[c][w++] = (signed char)loop[i + 1];
+                ++ntri;
+            }
+        }
+        t.count[c] = (unsigned char)ntri;
+    }
+}
+
+void mesh_tables_upload() {
+    static McTables tables;
+    static bool built = false;
+    if (!built) {
+        build_mc_tables(tables);
+        built = true;
+    }
+    cudaMemcpyToSymbol(c_edge_table, tables.edge, sizeof(tables.edge));
+    cudaMemcpyToSymbol(c_tri_table, tables.tri, sizeof(tables.tri));
+    cudaMemcpyToSymbol(c_tri_count, tables.count, sizeof(tables.count));
+}
+
+// ---------------------------------------------------------------- staging
+constexpr int kN = 9;            // staged cells per axis
+constexpr int kN3 = kN * kN * kN;
+
+// Stages block b's 9^3 neighbourhood: s[z*81 + y*9 + x] = sdf, or NaN when
+// the voxel is unobserved or its block is missing.
+template <int FMT>
+__device__ void stage_block(const MapDev &m, int b, int bx, int by, int bz, float *s) {
+    typedef VoxelIO<FMT> IO;
+    const typename IO::T *vox = static_cast<const typename IO::T *>(m.voxels);
+    __shared__ int nb[8];
+    if (threadIdx.x < 8) {
+        int c = threadIdx.x;
+        nb[c] = c == 0 ? b : find_block_xyz(m, bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1));
+    }
+    __syncthreads();
+    const float qnan = __int_as_float(0x7fffffff);
+    for (int i = threadIdx.x; i < kN3; i += blockDim.x) {
+        int x = i % kN, y = (i / kN) % kN, z = i / (kN * kN);
+        int c = (x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2);
+        int p = nb[c];
+        float v = qnan;
+        if (p >= 0) {
+            typename IO::T r = __ldg(vox + (size_t)p * kBlockVoxels + ((z & 7) << 6) + ((y & 7) << 3) + (x & 7));
+            if (IO::wt(r) != 0) v = IO::sdf(r);
+        }
+        s[i] = v;
+    }
+    __syncthreads();
+}
+
+// Case index of the cube at local (x,y,z); -1 when a corner is unobserved.
+__device__ __forceinline__ int cube_case(const float *s, int x, int y, int z, float sd[8]) {
+    int cidx = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int dx = (c == 1 || c == 2 || c == 5 || c == 6) ? 1 : 0;
+        const int dy = (c == 2 || c == 3 || c == 6 || c == 7) ? 1 : 0;
+        const int dz = c >= 4 ? 1 : 0;
+        float v = s[(z + dz) * 81 + (y + dy) * 9 + (x + dx)];
+        if (isnan(v)) return -1;
+        sd[c] = v;
+        if (v < 0.0f) cidx |= 1 << c;
+    }
+    return cidx;
+}
+
+__device__ __forceinline__ int cube_tris(int cidx) {
+    if (cidx <= 0) return 0;
+    if (c_edge_table[cidx] == 0) return 0;
+    return c_tri_count[cidx];
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(128) mc_count_kernel(MapDev m, unsigned nblocks, unsigned *block_tris) {
+    __shared__ float s[kN3];
+    __shared__ unsigned red[4];
+    for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        int bx, by, bz;
+        unpack_key(m.block_keys[b], bx, by, bz);
+        stage_block<FMT>(m, (int)b, bx, by, bz, s);
+        unsigned cnt = 0;
+        for (int i = threadIdx.x; i < kBlockVoxels; i += blockDim.x) {
+            float sd[8];
+            cnt += cube_tris(cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd));
+        }
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
+        __syncthreads();
+        if (threadIdx.x == 0) block_tris[b] = red[0] + red[1] + red[2] + red[3];
+        __syncthreads();
+    }
+}
+
+// Exclusive scan of per-block counts (single CTA; offsets[n] = total).
+__global__ void __launch_bounds__(1024) scan_kernel(const unsigned *in, unsigned *out, unsigned n,
+                                                    unsigned *total) {
+    __shared__ unsigned warp_sums[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (unsigned base = 0; base < n; base += blockDim.x) {
+        unsigned i = base + threadIdx.x;
+        unsigned v = i < n ? in[i] : 0u;
+        unsigned x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= (unsigned)o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warp_sums[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            unsigned w = warp_sums[threadIdx.x];
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= (unsigned)o) w += y;
+            }
+            warp_sums[threadIdx.x] = w;
+        }
+        __syncthreads();
+        unsigned wprefix = (threadIdx.x >= 32) ? warp_sums[(threadIdx.x >> 5) - 1] : 0u;
+        unsigned incl = x + wprefix;
+        if (i < n) out[i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[n] = carry;
+        *total = carry;
+    }
+}
+
+__device__ __forceinline__ float mc_interp(float v1, float v2) {
+    if (fabsf(0.0f - v1) < 1e-6f) return 0.0f;
+    if (fabsf(0.0f - v2) < 1e-6f) return 1.0f;
+    if (fabsf(v1 - v2) < 1e-6f) return 0.0f;
+    return (0.0f - v1) / (v2 - v1);
+}
+
+// Vertex on edge e of the cube at voxel position (px,py,pz), voxel units
+// (MeshEngine.cu:151-225).
+__device__ __forceinline__ float3 edge_vertex(int e, const float sd[8], float px, float py, float pz) {
+    switch (e) {
+        case 0: return make_float3(px + mc_interp(sd[0], sd[1]), py, pz);
+        case 1: return make_float3(px + 1.0f, py + mc_interp(sd[1], sd[2]), pz);
+        case 2: return make_float3(px + (1.0f - mc_interp(sd[2], sd[3])), py + 1.0f, pz);
+        case 3: return make_float3(px, py + (1.0f - mc_interp(sd[3], sd[0])), pz);
+        case 4: return make_float3(px + mc_interp(sd[4], sd[5]), py, pz + 1.0f);
+        case 5: return make_float3(px + 1.0f, py + mc_interp(sd[5], sd[6]), pz + 1.0f);
+        case 6: return make_float3(px + (1.0f - mc_interp(sd[6], sd[7])), py + 1.0f, pz + 1.0f);
+        case 7: return make_float3(px, py + (1.0f - mc_interp(sd[7], sd[4])), pz + 1.0f);
+        case 8: return make_float3(px, py, pz + mc_interp(sd[0], sd[4]));
+        case 9: return make_float3(px + 1.0f, py, pz + mc_interp(sd[1], sd[5]));
+        case 10: return make_float3(px + 1.0f, py + 1.0f, pz + mc_interp(sd[2], sd[6]));
+        default: return make_float3(px, py + 1.0f, pz + mc_interp(sd[3], sd[7]));
+    }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks,
+                                                      const unsigned *block_offset, int max_tris,
+                                                      float *points, float *normals, int *cases,
+                                                      int *cube_xyz) {
+    __shared__ float s[kN3];
+    __shared__ unsigned wsum[4];
+    const float vs = m.voxel_size;
+    for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        const unsigned base = block_offset[b];
+        if (block_offset[b + 1] == base) continue;  // uniform across the CTA
+        int bx, by, bz;
+        unpack_key(m.block_keys[b], bx, by, bz);
+        stage_block<FMT>(m, (int)b, bx, by, bz, s);
+        // each thread owns 4 consecutive cubes: i = 4*tid .. 4*tid+3
+        int cnt[4], cid[4];
+        unsigned mine = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int i = threadIdx.x * 4 + k;
+            float sd[8];
+            cid[k] = cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd);
+            cnt[k] = cube_tris(cid[k]);
+            mine += cnt[k];
+        }
+        unsigned incl = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((threadIdx.x & 31) >= (unsigned)o) incl += y;
+        }
+        if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = incl;
+        __syncthreads();
+        unsigned wpre = 0;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) wpre += wsum[w];
+        unsigned off = base + wpre + incl - mine;
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            if (cnt[k] == 0) continue;
+            int i = threadIdx.x * 4 + k;
+            int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
+            float sd[8];
+            cube_case(s, lx, ly, lz, sd);
+            const int gx = bx * 8 + lx, gy = by * 8 + ly, gz = bz * 8 + lz;
+            const float px = (float)gx, py = (float)gy, pz = (float)gz;
+            for (int t = 0; t < cnt[k]; ++t, ++off) {
+                if (off >= (unsigned)max_tris) continue;
+                float3 v[3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    float3 q = edge_vertex(c_tri_table[cid[k]][3 * t + j], sd, px, py, pz);
+                    v[j] = make_float3(q.x * vs, q.y * vs, q.z * vs);
+                }
+                float ax = v[1].x - v[0].x, ay = v[1].y - v[0].y, az = v[1].z - v[0].z;
+                float cx = v[2].x - v[0].x, cy = v[2].y - v[0].y, cz = v[2].z - v[0].z;
+                float nx = ay * cz - az * cy, ny = az * cx - ax * cz, nz = ax * cy - ay * cx;
+                float nn = nx * nx + ny * ny + nz * nz;
+                if (nn > 0.0f) {
+                    float inv = 1.0f / sqrtf(nn);
+                    nx *= inv;
+                    ny *= inv;
+                    nz *= inv;
+                }
+                float *pp = points + (size_t)off * 9;
+                float *nq = normals + (size_t)off * 9;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    pp[3 * j] = v[j].x;
+                    pp[3 * j + 1] = v[j].y;
+                    pp[3 * j + 2] = v[j].z;
+                    nq[3 * j] = nx;
+                    nq[3 * j + 1] = ny;
+                    nq[3 * j + 2] = nz;
+                }
+                cases[off] = cid[k];
+                cube_xyz[3 * off] = gx;
+                cube_xyz[3 * off + 1] = gy;
+                cube_xyz[3 * off + 2] = gz;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+int mesher_ensure_blocks(MeshBuffers &mb, size_t n_blocks) {
+    if (mb.cap_blocks >= n_blocks) return YAS_OK;
+    cudaFree(mb.block_tris);
+    cudaFree(mb.block_offset);
+    mb.block_tris = nullptr;
+    mb.block_offset = nullptr;
+    size_t cap = n_blocks < 1024 ? 1024 : n_blocks;
+    if (cudaMalloc(&mb.block_tris, cap * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&mb.block_offset, (cap + 1) * sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        mb.cap_blocks = 0;
+        return YAS_ERR_OOM;
+    }
+    mb.cap_blocks = cap;
+    return YAS_OK;
+}
+
+int launch_meshify(const MapDev &m, int fmt, MeshBuffers &mb, unsigned n_blocks, cudaStream_t s) {
+    YAS_TRY(mesher_ensure_blocks(mb, n_blocks));
+    cudaMemsetAsync(mb.counters, 0, sizeof(unsigned), s);
+    if (n_blocks == 0) return YAS_OK;
+    const unsigned grid = n_blocks < 152u * 16u ? n_blocks : 152u * 16u;
+    switch (fmt) {
+        case YAS_VOXEL_F32:
+            mc_count_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
+            break;
+        case YAS_VOXEL_F16:
+            mc_count_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
+            break;
+        default:
+            mc_count_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
+            break;
+    }
+    scan_kernel<<<1, 1024, 0, s>>>(mb.block_tris, mb.block_offset, n_blocks, mb.counters);
+    switch (fmt) {
+        case YAS_VOXEL_F32:
+            mc_emit_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+                                                               mb.points, mb.normals, mb.cases, mb.cube_xyz);
+            break;
+        case YAS_VOXEL_F16:
+            mc_emit_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+                                                               mb.points, mb.normals, mb.cases, mb.cube_xyz);
+            break;
+        default:
+            mc_emit_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+                                                               mb.points, mb.normals, mb.cases, mb.cube_xyz);
+            break;
+    }
+    return YAS_OK;
+}
+
+}  // namespace yas
+
+// Host-visible table access for tests (same generator as the device tables).
+extern "C" YAS_API int yas_mc_tables(unsigned short *edge, signed char *tri, unsigned char *count) {
+    yas::McTables t;
+    yas::build_mc_tables(t);
+    if (edge) memcpy(edge, t.edge, sizeof(t.edge));
+    if (tri) memcpy(tri, t.tri, sizeof(t.tri));
+    if (count) memcpy(count, t.count, sizeof(t.count));
+    return YAS_OK;
+}

@@ -1,0 +1,263 @@
+// raycast.cu — TSDF raycasting into a camera-frame vertex map.
+//
+// Reference semantics (paths relative to the reference project root):
+//   z-range tiles  RGBDFusion/src/RayTraceEngine.cu:58-214 (RenderingBlockDelegate,
+//                  FillRenderingBlockFunctor): every visible block's 8 corners are
+//                  projected to an (W/8)x(H/8) grid; each covered cell keeps the
+//                  min near / max far depth of the blocks covering it.
+//   ray march      RayTraceEngine.cu:266-410 (MapRenderingDelegate): march from the
+//                  cell's near to far depth in voxel units with step
+//                  max(sdf * trunc/voxel, 1) (1 when the sample is unobserved),
+//                  trilinear sampling when |sdf| <= 0.5, stop at sdf <= 0, then two
+//                  correction moves of sdf * trunc/voxel with one trilinear
+//                  re-sample between them.
+//
+// GB300 design: the z-range fill walks each visible block's footprint with
+// integer atomicMin/atomicMax on the float bit patterns (depths are positive,
+// so integer order equals float order) instead of CAS loops over split tiles;
+// the march caches the last block's pool index in registers, so consecutive
+// samples inside one 8^3 block cost one 4- or 8-byte load each.
+// Deliberate differences: a missed ray writes w = -1 (the reference leaves w
+// stale on its early return, RayTraceEngine.cu:338-347); the 8 trilinear
+// corners are floor(p) + {0,1}^3 (the reference floors p + offset per corner).
+#include <cfloat>
+
+#include "yas_internal.h"
+
+namespace yas {
+
+__global__ void zrange_reset_kernel(float *znear, float *zfar, int n, unsigned *n_render) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        znear[i] = 100.0f;
+        zfar[i] = 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_render = 0;
+}
+
+__device__ __forceinline__ int clamp_floor(float v) {
+    if (!(v > -1.0e6f)) return -1000000;
+    if (v > 1.0e6f) return 1000000;
+    return (int)floorf(v);
+}
+__device__ __forceinline__ int clamp_ceil(float v) {
+    if (!(v > -1.0e6f)) return -1000000;
+    if (v > 1.0e6f) return 1000000;
+    return (int)ceilf(v);
+}
+
+__global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, const PosePair *P,
+                                                          float *znear, float *zfar, int zw, int zh,
+                                                          const int *skip) {
+    if (skip && *skip) return;
+    const unsigned nvis = *(volatile unsigned *)&m.hdr->n_visible;
+    const Rigid32 Tinv = P->Tinv;
+    const float scale = m.voxel_size * 8.0f;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < nvis; j += gridDim.x * blockDim.x) {
+        int bx, by, bz;
+        unpack_key(m.block_keys[m.visible[j]], bx, by, bz);
+        int ulx = zw, uly = zh, lrx = -1, lry = -1;
+        float zmin = m.depth_max, zmax = m.depth_min;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            float3 p = rigid_exact(Tinv, (float)(bx + (c & 1)) * scale, (float)(by + ((c >> 1) & 1)) * scale,
+                                   (float)(bz + ((c >> 2) & 1)) * scale);
+            float u = (cam.fx * p.x / p.z + cam.cx) / 8.0f;
+            float v = (cam.fy * p.y / p.z + cam.cy) / 8.0f;
+            ulx = min(ulx, clamp_floor(u));
+            uly = min(uly, clamp_floor(v));
+            lrx = max(lrx, clamp_ceil(u));
+            lry = max(lry, clamp_ceil(v));
+            zmin = fminf(zmin, p.z);
+            zmax = fmaxf(zmax, p.z);
+        }
+        ulx = max(ulx, 0);
+        uly = max(uly, 0);
+        lrx = min(lrx, zw - 1);
+        lry = min(lry, zh - 1);
+        if (ulx > lrx || uly > lry) continue;
+        if (zmin < m.depth_min) zmin = m.depth_min;
+        if (zmax < m.depth_min) continue;
+        const int inear = __float_as_int(zmin), ifar = __float_as_int(zmax);
+        for (int y = uly; y <= lry; ++y)
+            for (int x = ulx; x <= lrx; ++x) {
+                atomicMin(reinterpret_cast<int *>(znear) + y * zw + x, inear);
+                atomicMax(reinterpret_cast<int *>(zfar) + y * zw + x, ifar);
+            }
+        unsigned tiles = (unsigned)(((lrx - ulx + 16) / 16) * ((lry - uly + 16) / 16));
+        atomicAdd(&m.hdr->n_render, tiles);
+    }
+}
+
+void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
+                   const int *skip, cudaStream_t s) {
+    int n = rb.zw * rb.zh;
+    zrange_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render);
+    zrange_fill_kernel<<<152 * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip);
+}
+
+// Block-pointer cache of one ray.
+template <int FMT>
+struct VoxelReader {
+    typedef VoxelIO<FMT> IO;
+    const MapDev &m;
+    const typename IO::T *vox;
+    unsigned long long ckey;
+    int cptr;
+    __device__ __forceinline__ VoxelReader(const MapDev &mm)
+        : m(mm), vox(static_cast<const typename IO::T *>(mm.voxels)), ckey(kEmptyKey), cptr(-1) {}
+
+    // sdf of voxel (vx,vy,vz); valid = observed (weight != 0)
+    __device__ __forceinline__ float read(int vx, int vy, int vz, bool &valid) {
+        int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;
+        unsigned long long k = pack_key(bx, by, bz);
+        if (k != ckey) {
+            ckey = k;
+            cptr = coord_in_range(bx, by, bz) ? find_block(m, k) : -1;
+        }
+        if (cptr < 0) {
+            valid = false;
+            return 1.0f;
+        }
+        typename IO::T v = __ldg(vox + (size_t)cptr * kBlockVoxels + ((vz & 7) << 6) + ((vy & 7) << 3) + (vx & 7));
+        if (IO::wt(v) == 0) {
+            valid = false;
+            return 1.0f;
+        }
+        valid = true;
+        return IO::sdf(v);
+    }
+    __device__ __forceinline__ float read_nearest(float3 p, bool &valid) {
+        return read((int)floorf(p.x), (int)floorf(p.y), (int)floorf(p.z), valid);
+    }
+    // Trilinear sample with the reference's lerp order (RayTraceEngine.cu:297-329).
+    __device__ __forceinline__ float read_interp(float3 p, bool &valid) {
+        float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+        int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+        float ax = p.x - fx, ay = p.y - fy, az = p.z - fz;
+        bool v0, v1, ok = true;
+        float s0 = read(x0, y0, z0, v0);
+        float s1 = read(x0 + 1, y0, z0, v1);
+        ok = v0 && v1;
+        float r0 = (1.0f - ax) * s0 + ax * s1;
+        s0 = read(x0, y0 + 1, z0, v0);
+        s1 = read(x0 + 1, y0 + 1, z0, v1);
+        ok = ok && v0 && v1;
+        float r1 = (1.0f - ax) * s0 + ax * s1;
+        float r2 = (1.0f - ay) * r0 + ay * r1;
+        s0 = read(x0, y0, z0 + 1, v0);
+        s1 = read(x0 + 1, y0, z0 + 1, v1);
+        ok = ok && v0 && v1;
+        r0 = (1.0f - ax) * s0 + ax * s1;
+        s0 = read(x0, y0 + 1, z0 + 1, v0);
+        s1 = read(x0 + 1, y0 + 1, z0 + 1, v1);
+        ok = ok && v0 && v1;
+        r1 = (1.0f - ax) * s0 + ax * s1;
+        float r3 = (1.0f - ay) * r0 + ay * r1;
+        valid = ok;
+        return (1.0f - az) * r2 + az * r3;
+    }
+};
+
+template <int FMT>
+__global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const PosePair *P,
+                                                    const float *__restrict__ znear,
+                                                    const float *__restrict__ zfar, int zw,
+                                                    float4 *vmap, int vpitch, const int *skip) {
+    const int x = blockIdx.x * 16 + (threadIdx.x & 15);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (x >= cam.w || y >= cam.h) return;
+    float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                             __int_as_float(0x7fffffff), -1.0f);
+    if (skip && *skip) {
+        vmap[(size_t)y * vpitch + x] = out;
+        return;
+    }
+    const float zn = __ldg(znear + (y >> 3) * zw + (x >> 3));
+    const float zf = __ldg(zfar + (y >> 3) * zw + (x >> 3));
+    if (!(zn < FLT_EPSILON || zf < FLT_EPSILON || isnan(zn) || isnan(zf))) {
+        const Rigid32 T = P->T;
+        const float vsinv = 1.0f / m.voxel_size;
+        const float rstep = m.trunc / m.voxel_size;
+        const float ux = cam.invfx * ((float)x - cam.cx), uy = cam.invfy * ((float)y - cam.cy);
+        float3 pn = make_float3(ux * zn, uy * zn, zn);
+        float dist_s = sqrtf(pn.x * pn.x + pn.y * pn.y + pn.z * pn.z) * vsinv;
+        float3 s = rigid_fast(T, pn.x, pn.y, pn.z);
+        s = make_float3(s.x * vsinv, s.y * vsinv, s.z * vsinv);
+        float3 pf = make_float3(ux * zf, uy * zf, zf);
+        const float dist_e = sqrtf(pf.x * pf.x + pf.y * pf.y + pf.z * pf.z) * vsinv;
+        float3 e = rigid_fast(T, pf.x, pf.y, pf.z);
+        e = make_float3(e.x * vsinv, e.y * vsinv, e.z * vsinv);
+        float3 dir = make_float3(e.x - s.x, e.y - s.y, e.z - s.z);
+        float dn = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+        if (dn > 0.0f) dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
+        float3 r = s;
+        VoxelReader<FMT> rd(m);
+        float sdf = 1.0f;
+        bool valid = false;
+        while (dist_s < dist_e) {
+            sdf = rd.read_nearest(r, valid);
+            if (sdf <= 0.5f && sdf >= -0.5f) sdf = rd.read_interp(r, valid);
+            if (sdf <= 0.0f) break;
+            float step = valid ? fmaxf(sdf * rstep, 1.0f) : 1.0f;
+            r.x += step * dir.x;
+            r.y += step * dir.y;
+            r.z += step * dir.z;
+            dist_s += step;
+        }
+        if (sdf <= 0.0f) {
+            float step = sdf * rstep;
+            r.x += step * dir.x;
+            r.y += step * dir.y;
+            r.z += step * dir.z;
+            sdf = rd.read_interp(r, valid);
+            step = sdf * rstep;
+            r.x += step * dir.x;
+            r.y += step * dir.y;
+            r.z += step * dir.z;
+            if (valid) {
+                const Rigid32 Ti = P->Tinv;
+                float3 w = make_float3(r.x / vsinv, r.y / vsinv, r.z / vsinv);
+                float3 c = rigid_fast(Ti, w.x, w.y, w.z);
+                out = make_float4(c.x, c.y, c.z, 1.0f);
+            }
+        }
+    }
+    vmap[(size_t)y * vpitch + x] = out;
+}
+
+void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
+                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
+    dim3 grid((cam.w + 15) / 16, (cam.h + 7) / 8);
+    switch (fmt) {
+        case YAS_VOXEL_F32:
+            march_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                             vmap_pitch_elems, skip);
+            break;
+        case YAS_VOXEL_F16:
+            march_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                             vmap_pitch_elems, skip);
+            break;
+        default:
+            march_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                             vmap_pitch_elems, skip);
+            break;
+    }
+}
+
+// VMapToDepth (ImageProc.cu:262-286): z of valid vertices, else 0.
+__global__ void vmap_to_depth_kernel(const float4 *vmap, int vpitch, float *depth, int dpitch, int w,
+                                     int h) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    float4 v = vmap[(size_t)y * vpitch + x];
+    depth[(size_t)y * dpitch + x] = v.w > 0.0f ? v.z : 0.0f;
+}
+
+void launch_vmap_to_depth(const float4 *vmap, int vpitch, float *depth, int dpitch, int w, int h,
+                          cudaStream_t s) {
+    dim3 grid((w + 127) / 128, h);
+    vmap_to_depth_kernel<<<grid, 128, 0, s>>>(vmap, vpitch, depth, dpitch, w, h);
+}
+
+}  // namespace yas

@@ -1,0 +1,432 @@
+// session.cu — one SLAM session's per-frame dense pipeline as a CUDA graph.
+//
+// Reference flow (paths relative to the reference project root):
+//   first frame   FullSystem/src/Tracking.cpp:139-155 (StereoInitialization):
+//                 SetReferenceImage, SetReferenceDepth, Fuse(depth, identity).
+//   later frames  Tracking.cpp:162-197 (TrackRGBD): RayTrace(Tcm_last) ->
+//                 SetReferenceModel(vmap) -> SetTrackingImage/Depth ->
+//                 DT = GetTransform(identity, swap) -> reject |t(DT)| > 0.1 m ->
+//                 Tcm = Tcm_last * DT^-1 -> Fuse(depth, Tcm).
+//   colour/depth  FullSystem/src/System.cpp:43-65 (RGB -> gray, u16 -> metres).
+//
+// GB300 design: the whole frame (preprocessing, raycast, model pyramid, every
+// Gauss-Newton iteration with its device-side solve, the frame-step check,
+// the pose update, block allocation, visibility and integration) is one
+// captured graph; the only host traffic per frame is the input upload before
+// the graph and one 200-byte frame record copied back at its end.  The frame
+// step check and pose composition run on the device, and fusion kernels read
+// a skip flag, so a rejected frame changes nothing.  The raycast reuses the
+// visible-block list of the previous fusion, which was built at exactly the
+// pose the raycast uses.  Two graphs alternate because the reference and
+// current pyramids swap roles every frame (RGBDTracking::SwapFrameBuffer,
+// RGBDTracking.cu:294-303).
+// Deliberate difference: a NaN in the solve skips fusion and reports
+// YAS_ERR_NUMERIC (the reference fuses at the previous pose).
+#include <cstring>
+
+#include "yas_track.h"
+
+namespace yas {
+
+struct __align__(16) FrameState {
+    PosePair pp;      // current Tcm in float (T) and its inverse (Tinv)
+    double Tcm[12];   // current Tcm, row-major [R|t]
+    double dt[12];    // last frame step DT (current <- previous)
+    int skip;         // 1: fusion kernels return immediately
+    int status;       // yas_status of the last frame
+    int frame;        // frames processed
+    int pad;
+};
+
+__device__ void publish_pose(FrameState *fs) {
+    const double *T = fs->Tcm;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            fs->pp.T.r[i * 3 + j] = (float)T[i * 4 + j];
+            fs->pp.Tinv.r[i * 3 + j] = (float)T[j * 4 + i];
+        }
+        fs->pp.T.t[i] = (float)T[i * 4 + 3];
+    }
+    for (int i = 0; i < 3; ++i)
+        fs->pp.Tinv.t[i] = (float)(-((T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7]) + T[2 * 4 + i] * T[11]));
+}
+
+__global__ void frame_begin_kernel(FrameState *fs, Pose64 init, MapHeader *hdr) {
+    if (threadIdx.x != 0) return;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) fs->Tcm[i * 4 + j] = init.r[i * 3 + j];
+        fs->Tcm[i * 4 + 3] = init.t[i];
+    }
+    for (int i = 0; i < 12; ++i) fs->dt[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    publish_pose(fs);
+    fs->skip = 0;
+    fs->status = YAS_OK;
+    fs->frame = 1;
+    hdr->n_visible = 0;
+}
+
+// Frame-step check and pose composition: Tcm <- Tcm * DT^-1 (Tracking.cpp:178-187).
+__global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float max_t, MapHeader *hdr) {
+    if (threadIdx.x != 0) return;
+    fs->frame += 1;
+    if (st->failed) {
+        fs->status = YAS_ERR_NUMERIC;
+        fs->skip = 1;
+        return;
+    }
+    const double *D = st->best;
+    for (int i = 0; i < 12; ++i) fs->dt[i] = D[i];
+    const double tn = sqrt(D[3] * D[3] + D[7] * D[7] + D[11] * D[11]);
+    if (!(tn <= (double)max_t)) {
+        fs->status = YAS_ERR_TRACK_LOST;
+        fs->skip = 1;
+        return;
+    }
+    // DT^-1 = [R^T | -R^T t]
+    double Di[12];
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) Di[i * 4 + j] = D[j * 4 + i];
+        Di[i * 4 + 3] = -((D[0 * 4 + i] * D[3] + D[1 * 4 + i] * D[7]) + D[2 * 4 + i] * D[11]);
+    }
+    double o[12];
+    const double *A = fs->Tcm;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            o[i * 4 + j] = (A[i * 4 + 0] * Di[0 * 4 + j] + A[i * 4 + 1] * Di[1 * 4 + j]) + A[i * 4 + 2] * Di[2 * 4 + j];
+        o[i * 4 + 3] = ((A[i * 4 + 0] * Di[3] + A[i * 4 + 1] * Di[7]) + A[i * 4 + 2] * Di[11]) + A[i * 4 + 3];
+    }
+    for (int i = 0; i < 12; ++i) fs->Tcm[i] = o[i];
+    publish_pose(fs);
+    fs->skip = 0;
+    fs->status = YAS_OK;
+    hdr->n_visible = 0;
+}
+
+}  // namespace yas
+
+using namespace yas;
+
+struct yas_session {
+    yas_session_config cfg;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    yas_map *map = nullptr;
+    yas_raycaster *rc = nullptr;
+    yas_tracker *tr = nullptr;
+    uint8_t *d_rgb = nullptr;
+    uint16_t *d_depth = nullptr;
+    float *d_depth_m = nullptr;
+    FrameState *fs = nullptr;
+    FrameState *fs_host = nullptr;
+    int frames = 0;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int kernels_per_frame = 0;
+    Cam cam;
+    // profiling: events recorded between launches of an eager frame
+    std::vector<cudaEvent_t> prof_events;
+    std::vector<int> prof_ids;
+    bool profiling = false;
+};
+
+// Records an event tagged `id` before the next launch (profiling only).
+static void prof_mark(void *ctx, int id) {
+    yas_session *s = static_cast<yas_session *>(ctx);
+    if (!s->profiling) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, s->stream);
+    s->prof_events.push_back(e);
+    s->prof_ids.push_back(id);
+}
+
+// Stage ids of the profiling marks (pass A / B of level l are 10+l / 20+l).
+enum { kStImage = 0, kStDepth = 1, kStZrange = 2, kStMarch = 3, kStModel = 4, kStGnInit = 5,
+       kStFinalize = 6, kStAllocate = 7, kStVisible = 8, kStIntegrate = 9, kStEnd = 99 };
+
+static void enqueue_fusion(yas_session *s, const int *skip) {
+    MapDev v = map_view(s->map);
+    const int fmt = s->map->cfg.voxel_format;
+    prof_mark(s, kStAllocate);
+    launch_allocate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream);
+    prof_mark(s, kStVisible);
+    launch_visible(v, s->cam, &s->fs->pp, skip, s->stream);
+    prof_mark(s, kStIntegrate);
+    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream);
+}
+
+static void enqueue_first_frame(yas_session *s) {
+    yas_tracker *tr = s->tr;
+    tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, true, s->stream);
+    tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, true, s->stream);
+    frame_begin_kernel<<<1, 32, 0, s->stream>>>(s->fs, pose_identity(), s->map->hdr);
+    enqueue_fusion(s, nullptr);
+    cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, s->stream);
+}
+
+static void enqueue_tracked_frame(yas_session *s) {
+    yas_tracker *tr = s->tr;
+    cudaStream_t st = s->stream;
+    prof_mark(s, kStImage);
+    tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, false, st);
+    prof_mark(s, kStDepth);
+    tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, false, st);
+    MapDev v = map_view(s->map);
+    prof_mark(s, kStZrange);
+    launch_zrange(v, s->rc->cam, &s->fs->pp, s->rc->rb, nullptr, st);
+    prof_mark(s, kStMarch);
+    launch_march(v, s->map->cfg.voxel_format, s->rc->cam, &s->fs->pp, s->rc->rb, tr->refb(0).vmap, s->cfg.width,
+                 nullptr, st);
+    prof_mark(s, kStModel);
+    tracker_model(tr, st);
+    prof_mark(s, kStGnInit);
+    launch_gn_init(tr, pose_identity(), st);
+    launch_gn_schedule(tr, st);
+    prof_mark(s, kStFinalize);
+    frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, tr->state, s->cfg.max_step_translation, s->map->hdr);
+    enqueue_fusion(s, &s->fs->skip);
+    prof_mark(s, kStEnd);
+    cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, st);
+}
+
+static int count_kernel_nodes(cudaGraph_t g, int *out) {
+    size_t n = 0;
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    int k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        YAS_TRY_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    *out = k;
+    return YAS_OK;
+}
+
+static int build_graph(yas_session *s, int parity) {
+    cudaGraph_t g = nullptr;
+    YAS_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_tracked_frame(s);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (e != cudaSuccess) {
+        record_cuda_error(e, "graph capture", __FILE__, __LINE__);
+        if (g) cudaGraphDestroy(g);
+        return YAS_ERR_CUDA;
+    }
+    int st = count_kernel_nodes(g, &s->kernels_per_frame);
+    if (st == YAS_OK) {
+        e = cudaGraphInstantiate(&s->exec[parity], g, 0);
+        if (e != cudaSuccess) {
+            record_cuda_error(e, "graph instantiate", __FILE__, __LINE__);
+            st = YAS_ERR_CUDA;
+        }
+    }
+    cudaGraphDestroy(g);
+    return st;
+}
+
+extern "C" {
+
+YAS_API int yas_session_config_default(yas_session_config *cfg, int width, int height, const yas_intrinsics *K,
+                                       int hash_slots, int max_blocks, float voxel_size, float trunc_dist,
+                                       int voxel_format) {
+    if (!cfg || !K) return YAS_ERR_BAD_ARG;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->width = width;
+    cfg->height = height;
+    cfg->K = *K;
+    yas_map_config_default(&cfg->map, hash_slots, max_blocks, voxel_size, trunc_dist, voxel_format);
+    cfg->num_levels = 3;
+    const int it[5] = {10, 5, 3, 3, 3};
+    for (int i = 0; i < 5; ++i) cfg->iterations[i] = it[i];
+    cfg->mode = YAS_TRACK_RGBD;
+    cfg->depth_scale = 0.001f;
+    cfg->max_step_translation = 0.1f;
+    cfg->use_graph = 1;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_destroy(yas_session *s);
+
+YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg, void *stream) {
+    if (!out || !cfg || cfg->width <= 0 || cfg->height <= 0) return YAS_ERR_BAD_ARG;
+    *out = nullptr;
+    yas_session *s = new yas_session();
+    s->cfg = *cfg;
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            delete s;
+            return YAS_ERR_CUDA;
+        }
+        s->own_stream = true;
+    }
+    s->cam = make_cam(cfg->K.fx, cfg->K.fy, cfg->K.cx, cfg->K.cy, cfg->width, cfg->height);
+    int st = yas_map_create(&s->map, &cfg->map, &cfg->K, s->stream);
+    if (st == YAS_OK) st = yas_raycaster_create(&s->rc, cfg->width, cfg->height, &cfg->K, s->stream);
+    if (st == YAS_OK) {
+        const double K[9] = {cfg->K.fx, 0, cfg->K.cx, 0, cfg->K.fy, cfg->K.cy, 0, 0, 1};
+        st = yas_tracker_create(&s->tr, cfg->width, cfg->height, K, cfg->num_levels, cfg->iterations, cfg->mode,
+                                s->stream);
+    }
+    if (st == YAS_OK) {
+        const size_t n = (size_t)cfg->width * cfg->height;
+        if (cudaMalloc(&s->d_rgb, n * 3) != cudaSuccess || cudaMalloc(&s->d_depth, n * 2) != cudaSuccess ||
+            cudaMalloc(&s->d_depth_m, n * 4) != cudaSuccess || cudaMalloc(&s->fs, sizeof(FrameState)) != cudaSuccess ||
+            cudaMallocHost(&s->fs_host, sizeof(FrameState)) != cudaSuccess) {
+            cudaGetLastError();
+            st = YAS_ERR_OOM;
+        } else {
+            cudaMemsetAsync(s->fs, 0, sizeof(FrameState), s->stream);
+            memset(s->fs_host, 0, sizeof(FrameState));
+        }
+    }
+    if (st == YAS_OK) {
+        s->tr->hook = prof_mark;
+        s->tr->hook_ctx = s;
+    }
+    if (st == YAS_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) st = YAS_ERR_CUDA;
+    if (st != YAS_OK) {
+        yas_session_destroy(s);
+        return st;
+    }
+    *out = s;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_destroy(yas_session *s) {
+    if (!s) return YAS_ERR_BAD_ARG;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int i = 0; i < 2; ++i)
+        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+    if (s->tr) yas_tracker_destroy(s->tr);
+    if (s->rc) yas_raycaster_destroy(s->rc);
+    if (s->map) yas_map_destroy(s->map);
+    cudaFree(s->d_rgb);
+    cudaFree(s->d_depth);
+    cudaFree(s->d_depth_m);
+    cudaFree(s->fs);
+    if (s->fs_host) cudaFreeHost(s->fs_host);
+    if (s->own_stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_submit(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device) {
+    if (!s || !rgb || !depth) return YAS_ERR_BAD_ARG;
+    const size_t n = (size_t)s->cfg.width * s->cfg.height;
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_depth, depth, n * 2, kind, s->stream));
+    if (s->frames == 0) {
+        enqueue_first_frame(s);
+    } else if (s->cfg.use_graph) {
+        const int parity = s->tr->cur;
+        if (!s->exec[parity]) YAS_TRY(build_graph(s, parity));
+        YAS_TRY_CUDA(cudaGraphLaunch(s->exec[parity], s->stream));
+        s->tr->cur = 1 - s->tr->cur;
+    } else {
+        enqueue_tracked_frame(s);
+        s->tr->cur = 1 - s->tr->cur;
+    }
+    YAS_TRY_CUDA(cudaGetLastError());
+    s->frames++;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_wait(yas_session *s, yas_pose *out_Tcm, int *out_status) {
+    if (!s) return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaStreamSynchronize(s->stream));
+    if (out_Tcm)
+        for (int i = 0; i < 12; ++i) out_Tcm->m[i] = s->fs_host->Tcm[i];
+    if (out_status) *out_status = s->fs_host->status;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_process_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device,
+                                      yas_pose *out_Tcm, int *out_status) {
+    YAS_TRY(yas_session_submit(s, rgb, depth, on_device));
+    return yas_session_wait(s, out_Tcm, out_status);
+}
+
+YAS_API int yas_session_map(yas_session *s, yas_map **out) {
+    if (!s || !out) return YAS_ERR_BAD_ARG;
+    *out = s->map;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_tracker(yas_session *s, yas_tracker **out) {
+    if (!s || !out) return YAS_ERR_BAD_ARG;
+    *out = s->tr;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_raycaster(yas_session *s, yas_raycaster **out) {
+    if (!s || !out) return YAS_ERR_BAD_ARG;
+    *out = s->rc;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_frame_count(yas_session *s, int *out) {
+    if (!s || !out) return YAS_ERR_BAD_ARG;
+    *out = s->frames;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_depth(yas_session *s, const float **dev_depth, int *pitch_bytes) {
+    if (!s || !dev_depth) return YAS_ERR_BAD_ARG;
+    *dev_depth = s->d_depth_m;
+    if (pitch_bytes) *pitch_bytes = s->cfg.width * 4;
+    return YAS_OK;
+}
+
+YAS_API int yas_session_kernels_per_frame(yas_session *s, int *out) {
+    if (!s || !out) return YAS_ERR_BAD_ARG;
+    *out = s->kernels_per_frame;
+    return YAS_OK;
+}
+
+YAS_API void *yas_session_stream(yas_session *s) { return s ? (void *)s->stream : nullptr; }
+
+YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device,
+                                      int *stage_ids, float *stage_ms, int capacity, int *out_count) {
+    if (!s || !rgb || !depth || !out_count) return YAS_ERR_BAD_ARG;
+    if (s->frames == 0) return YAS_ERR_STATE;  // the first frame initialises, it is not a tracked frame
+    const size_t n = (size_t)s->cfg.width * s->cfg.height;
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_depth, depth, n * 2, kind, s->stream));
+    s->profiling = true;
+    enqueue_tracked_frame(s);
+    s->profiling = false;
+    s->tr->cur = 1 - s->tr->cur;
+    s->frames++;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    int st = YAS_OK;
+    if (e != cudaSuccess) {
+        record_cuda_error(e, "profile frame", __FILE__, __LINE__);
+        st = YAS_ERR_CUDA;
+    }
+    const int m = (int)s->prof_events.size() - 1;
+    int k = 0;
+    for (int i = 0; i < m && st == YAS_OK; ++i) {
+        if (k >= capacity) {
+            st = YAS_ERR_CAPACITY;
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, s->prof_events[i], s->prof_events[i + 1]);
+        if (stage_ids) stage_ids[k] = s->prof_ids[i];
+        if (stage_ms) stage_ms[k] = ms;
+        ++k;
+    }
+    for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
+    s->prof_events.clear();
+    s->prof_ids.clear();
+    *out_count = k;
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,243 @@
+// yas_common.cuh — device helpers shared by every kernel of the dense path.
+//
+// Contents:
+//  * canonical FP32 arithmetic for the discrete decisions (block allocation,
+//    visibility, pixel selection): every product and sum is rounded on its
+//    own (no FMA contraction), in a fixed order, so the CPU oracle compiled
+//    with -ffp-contract=off reproduces each decision bit for bit;
+//  * 64-bit block keys (21-bit signed x,y,z) and the open-addressing hash
+//    table of 16-byte slots that replaces the reference's bucket + excess
+//    list table (RGBDFusion/utils/VoxelStructUtils.h:16-21, 173-317);
+//  * the three voxel storage formats;
+//  * MapDev, the by-value kernel view of one map.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/yas.h"
+
+namespace yas {
+
+constexpr int kBlockSide = 8;      // voxels per block edge (VoxelMap.h:12)
+constexpr int kBlockVoxels = 512;  // voxels per block (VoxelMap.h:13)
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr int kMaxProbes = 2048;   // bounded linear probing (no unbounded spin)
+constexpr int kCoordBits = 21;
+constexpr int kCoordMax = (1 << (kCoordBits - 1)) - 1;   // 1048575
+constexpr int kCoordMin = -(1 << (kCoordBits - 1));      // -1048576
+
+// Sticky error bits written by kernels into MapHeader::err_bits.
+__host__ __device__ constexpr unsigned err_bit(int code) { return 1u << code; }
+
+// ------------------------------------------------------------------ FP32 canon
+__device__ __forceinline__ float cmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float cadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float csub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float cdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// Row-major rotation + translation in float (converted from a double pose on
+// the host or device by round-to-nearest of each element).
+struct Rigid32 {
+    float r[9];
+    float t[3];
+};
+
+// y = R x + t with the canonical order ((r0 x + r1 y) + r2 z) + t0.
+__device__ __forceinline__ float3 rigid_exact(const Rigid32 &T, float x, float y, float z) {
+    float3 o;
+    o.x = cadd(cadd(cadd(cmul(T.r[0], x), cmul(T.r[1], y)), cmul(T.r[2], z)), T.t[0]);
+    o.y = cadd(cadd(cadd(cmul(T.r[3], x), cmul(T.r[4], y)), cmul(T.r[5], z)), T.t[1]);
+    o.z = cadd(cadd(cadd(cmul(T.r[6], x), cmul(T.r[7], y)), cmul(T.r[8], z)), T.t[2]);
+    return o;
+}
+
+// Fast form (FMA allowed) for continuous quantities compared with tolerance.
+__device__ __forceinline__ float3 rigid_fast(const Rigid32 &T, float x, float y, float z) {
+    return make_float3(fmaf(T.r[0], x, fmaf(T.r[1], y, fmaf(T.r[2], z, T.t[0]))),
+                       fmaf(T.r[3], x, fmaf(T.r[4], y, fmaf(T.r[5], z, T.t[1]))),
+                       fmaf(T.r[6], x, fmaf(T.r[7], y, fmaf(T.r[8], z, T.t[2]))));
+}
+
+__device__ __forceinline__ float3 rotate_fast(const Rigid32 &T, float x, float y, float z) {
+    return make_float3(fmaf(T.r[0], x, fmaf(T.r[1], y, T.r[2] * z)),
+                       fmaf(T.r[3], x, fmaf(T.r[4], y, T.r[5] * z)),
+                       fmaf(T.r[6], x, fmaf(T.r[7], y, T.r[8] * z)));
+}
+
+// floor division by the block side for voxel -> block, and the local index
+// z*64 + y*8 + x (VoxelStructUtils.h:28-72).
+__device__ __forceinline__ int floor_div8(int v) { return v >> 3; }  // arithmetic shift == floor
+__device__ __forceinline__ int mod8(int v) { return v & 7; }
+
+// ------------------------------------------------------------------ keys/hash
+__host__ __device__ __forceinline__ unsigned long long pack_key(int x, int y, int z) {
+    return ((unsigned long long)(x & 0x1FFFFF) << 42) | ((unsigned long long)(y & 0x1FFFFF) << 21) |
+           (unsigned long long)(z & 0x1FFFFF);
+}
+__host__ __device__ __forceinline__ int sext21(unsigned v) {
+    return (int)(v << 11) >> 11;
+}
+__host__ __device__ __forceinline__ void unpack_key(unsigned long long k, int &x, int &y, int &z) {
+    x = sext21((unsigned)((k >> 42) & 0x1FFFFF));
+    y = sext21((unsigned)((k >> 21) & 0x1FFFFF));
+    z = sext21((unsigned)(k & 0x1FFFFF));
+}
+__host__ __device__ __forceinline__ bool coord_in_range(int x, int y, int z) {
+    return x >= kCoordMin && x <= kCoordMax && y >= kCoordMin && y <= kCoordMax &&
+           z >= kCoordMin && z <= kCoordMax;
+}
+// 64-bit finaliser of MurmurHash3 (Appleby), used as the slot hash.
+__host__ __device__ __forceinline__ unsigned hash_key(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return (unsigned)k;
+}
+
+// One hash-table slot: 16 bytes, read with a single 128-bit load.
+struct __align__(16) HashSlot {
+    unsigned long long key;  // kEmptyKey when free
+    int ptr;                 // block index in the pool, -1 until assigned
+    int pad;
+};
+
+// Device-resident counters of one map.
+struct __align__(16) MapHeader {
+    unsigned n_alloc;       // bump counter of the block pool (may pass max_blocks on overflow)
+    unsigned n_visible;     // length of the visible list
+    unsigned err_bits;      // sticky yas_status bits
+    unsigned n_alloc_prev;  // n_alloc before the latest allocation pass
+    unsigned n_render;      // raycast: z-range tiles written
+    unsigned pad[3];
+};
+
+// ------------------------------------------------------------------ formats
+template <int FMT>
+struct VoxelIO;
+
+template <>
+struct VoxelIO<YAS_VOXEL_F32> {
+    typedef float2 T;
+    static constexpr int kBytes = 8;
+    __device__ __forceinline__ static float sdf(T v) { return v.x; }
+    __device__ __forceinline__ static int wt(T v) { return (int)v.y; }
+    __device__ __forceinline__ static T make(float s, int w) { return make_float2(s, (float)w); }
+};
+
+template <>
+struct VoxelIO<YAS_VOXEL_F16> {
+    typedef unsigned T;
+    static constexpr int kBytes = 4;
+    __device__ __forceinline__ static float sdf(T v) {
+        return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+    }
+    __device__ __forceinline__ static int wt(T v) { return (int)(v >> 16); }
+    __device__ __forceinline__ static T make(float s, int w) {
+        return (unsigned)__half_as_ushort(__float2half_rn(s)) | ((unsigned)w << 16);
+    }
+};
+
+template <>
+struct VoxelIO<YAS_VOXEL_S24> {
+    typedef unsigned T;
+    static constexpr int kBytes = 4;
+    __device__ __forceinline__ static float sdf(T v) {
+        return (float)((int)v >> 8) * (1.0f / 4194304.0f);
+    }
+    __device__ __forceinline__ static int wt(T v) { return (int)(v & 0xffu); }
+    __device__ __forceinline__ static T make(float s, int w) {
+        int q = __float2int_rn(s * 4194304.0f);
+        q = max(-8388608, min(8388607, q));
+        return ((unsigned)q << 8) | ((unsigned)w & 0xffu);
+    }
+};
+
+// ------------------------------------------------------------------ map view
+struct MapDev {
+    HashSlot *slots;
+    unsigned slot_mask;
+    unsigned long long *block_keys;  // [max_blocks] key of each pool block
+    void *voxels;                    // [max_blocks * 512] in the map's format
+    int *visible;                    // [max_blocks] compacted visible block indices
+    MapHeader *hdr;
+    int max_blocks;
+    float voxel_size;
+    float trunc;
+    float depth_min;
+    float depth_max;
+    int max_weight;
+};
+
+__device__ __forceinline__ unsigned num_blocks(const MapDev &m) {
+    unsigned n = *(volatile unsigned *)&m.hdr->n_alloc;
+    return n < (unsigned)m.max_blocks ? n : (unsigned)m.max_blocks;
+}
+
+// Read-only lookup: block index of key, or -1 (VoxelStructUtils.h:282-300).
+__device__ __forceinline__ int find_block(const MapDev &m, unsigned long long key) {
+    unsigned s = hash_key(key) & m.slot_mask;
+#pragma unroll 1
+    for (int i = 0; i < kMaxProbes; ++i) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(m.slots + s));
+        if (v.x == key) return (int)(unsigned)(v.y & 0xffffffffull);
+        if (v.x == kEmptyKey) return -1;
+        s = (s + 1) & m.slot_mask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int find_block_xyz(const MapDev &m, int bx, int by, int bz) {
+    if (!coord_in_range(bx, by, bz)) return -1;
+    return find_block(m, pack_key(bx, by, bz));
+}
+
+// Claims a slot for `key`: returns 1 if this call inserted it (slot index in
+// *slot_out), 0 if the key was already present, -1 if the probe limit was hit.
+__device__ __forceinline__ int claim_slot(const MapDev &m, unsigned long long key, unsigned *slot_out) {
+    unsigned s = hash_key(key) & m.slot_mask;
+#pragma unroll 1
+    for (int i = 0; i < kMaxProbes; ++i) {
+        unsigned long long k = __ldcg(&m.slots[s].key);
+        if (k == key) return 0;
+        if (k == kEmptyKey) {
+            unsigned long long prev = atomicCAS(&m.slots[s].key, kEmptyKey, key);
+            if (prev == kEmptyKey) {
+                *slot_out = s;
+                return 1;
+            }
+            if (prev == key) return 0;
+        }
+        s = (s + 1) & m.slot_mask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void raise_error(const MapDev &m, int code) {
+    atomicOr(&m.hdr->err_bits, err_bit(code));
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+// Warp-aggregated append: every lane with `pred` gets a unique index into a
+// list whose length lives at *counter; one atomicAdd per warp.  All 32 lanes
+// of the warp must call it together.
+__device__ __forceinline__ unsigned warp_append(unsigned *counter, bool pred) {
+    unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return 0xffffffffu;
+    int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return pred ? base + (unsigned)__popc(mask & lanemask_lt()) : 0xffffffffu;
+}
+
+}  // namespace yas
