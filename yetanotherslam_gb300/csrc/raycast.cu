@@ -191,11 +191,40 @@ __global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const Pos
         float dn = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
         if (dn > 0.0f) dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
         float3 r = s;
+        const float3 idir = make_float3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f,
+                                        dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+        unsigned long long skipped = kEmptyKey;
         VoxelReader<FMT> rd(m);
         float sdf = 1.0f;
         bool valid = false;
         while (dist_s < dist_e) {
             sdf = rd.read_nearest(r, valid);
+            if (rd.cptr < 0 && rd.ckey != skipped) {
+                // Unallocated block: every sample until the ray leaves it reads
+                // "unobserved" and advances one voxel, so those samples are
+                // skipped in one move.  k = steps to the first sample outside
+                // the block on the earliest exit axis; two are kept as margin
+                // against rounding, so the samples evaluated next are the last
+                // ones inside the block (evaluated normally).
+                skipped = rd.ckey;
+                const float bx0 = floorf(floorf(r.x) * 0.125f) * 8.0f;
+                const float by0 = floorf(floorf(r.y) * 0.125f) * 8.0f;
+                const float bz0 = floorf(floorf(r.z) * 0.125f) * 8.0f;
+                const float kx = dir.x > 0.0f ? ceilf((bx0 + 8.0f - r.x) * idir.x)
+                                              : (dir.x < 0.0f ? floorf((bx0 - r.x) * idir.x) + 1.0f : 1e30f);
+                const float ky = dir.y > 0.0f ? ceilf((by0 + 8.0f - r.y) * idir.y)
+                                              : (dir.y < 0.0f ? floorf((by0 - r.y) * idir.y) + 1.0f : 1e30f);
+                const float kz = dir.z > 0.0f ? ceilf((bz0 + 8.0f - r.z) * idir.z)
+                                              : (dir.z < 0.0f ? floorf((bz0 - r.z) * idir.z) + 1.0f : 1e30f);
+                const float n = fminf(fminf(fminf(kx, ky), kz) - 2.0f, ceilf(dist_e - dist_s));
+                if (n >= 1.0f) {
+                    r.x += n * dir.x;
+                    r.y += n * dir.y;
+                    r.z += n * dir.z;
+                    dist_s += n;
+                    continue;
+                }
+            }
             if (sdf <= 0.5f && sdf >= -0.5f) sdf = rd.read_interp(r, valid);
             if (sdf <= 0.0f) break;
             float step = valid ? fmaxf(sdf * rstep, 1.0f) : 1.0f;

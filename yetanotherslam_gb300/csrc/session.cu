@@ -38,68 +38,84 @@ struct __align__(16) FrameState {
     int pad;
 };
 
-__device__ void publish_pose(FrameState *fs) {
+// Float pose pair of fs->Tcm, one lane per entry (lanes 0..11).
+__device__ void publish_pose(FrameState *fs, int lane) {
     const double *T = fs->Tcm;
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j) {
+    if (lane < 12) {
+        const int i = lane / 4, j = lane % 4;
+        if (j < 3) {
             fs->pp.T.r[i * 3 + j] = (float)T[i * 4 + j];
             fs->pp.Tinv.r[i * 3 + j] = (float)T[j * 4 + i];
+        } else {
+            fs->pp.T.t[i] = (float)T[i * 4 + 3];
+            fs->pp.Tinv.t[i] = (float)(-((T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7]) + T[2 * 4 + i] * T[11]));
         }
-        fs->pp.T.t[i] = (float)T[i * 4 + 3];
     }
-    for (int i = 0; i < 3; ++i)
-        fs->pp.Tinv.t[i] = (float)(-((T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7]) + T[2 * 4 + i] * T[11]));
 }
 
 __global__ void frame_begin_kernel(FrameState *fs, Pose64 init, MapHeader *hdr) {
-    if (threadIdx.x != 0) return;
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j) fs->Tcm[i * 4 + j] = init.r[i * 3 + j];
-        fs->Tcm[i * 4 + 3] = init.t[i];
+    const int lane = threadIdx.x;
+    if (lane < 12) {
+        const int i = lane / 4, j = lane % 4;
+        fs->Tcm[lane] = j < 3 ? init.r[i * 3 + j] : init.t[i];
+        fs->dt[lane] = (lane % 5 == 0) ? 1.0 : 0.0;
     }
-    for (int i = 0; i < 12; ++i) fs->dt[i] = (i % 5 == 0) ? 1.0 : 0.0;
-    publish_pose(fs);
-    fs->skip = 0;
-    fs->status = YAS_OK;
-    fs->frame = 1;
-    hdr->n_visible = 0;
+    __syncwarp();
+    publish_pose(fs, lane);
+    if (lane == 0) {
+        fs->skip = 0;
+        fs->status = YAS_OK;
+        fs->frame = 1;
+        hdr->n_visible = 0;
+    }
 }
 
-// Frame-step check and pose composition: Tcm <- Tcm * DT^-1 (Tracking.cpp:178-187).
+// Frame-step check and pose composition: Tcm <- Tcm * DT^-1 (Tracking.cpp:178-187),
+// one warp, one lane per matrix entry (FP64 issues at the same cost for one or
+// 32 active lanes on GB300).
 __global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float max_t, MapHeader *hdr) {
-    if (threadIdx.x != 0) return;
-    fs->frame += 1;
-    if (st->failed) {
-        fs->status = YAS_ERR_NUMERIC;
-        fs->skip = 1;
-        return;
-    }
+    const int lane = threadIdx.x;
+    __shared__ double Di[12], A[12];
+    __shared__ int ok;
     const double *D = st->best;
-    for (int i = 0; i < 12; ++i) fs->dt[i] = D[i];
-    const double tn = sqrt(D[3] * D[3] + D[7] * D[7] + D[11] * D[11]);
-    if (!(tn <= (double)max_t)) {
-        fs->status = YAS_ERR_TRACK_LOST;
-        fs->skip = 1;
-        return;
+    if (lane == 0) {
+        fs->frame += 1;
+        // |t| > max_t, compared squared (no FP64 square root)
+        const double tn2 = D[3] * D[3] + D[7] * D[7] + D[11] * D[11];
+        ok = 1;
+        if (st->failed) {
+            fs->status = YAS_ERR_NUMERIC;
+            fs->skip = 1;
+            ok = 0;
+        } else if (!(tn2 <= (double)max_t * (double)max_t)) {
+            fs->status = YAS_ERR_TRACK_LOST;
+            fs->skip = 1;
+            ok = 0;
+        }
     }
-    // DT^-1 = [R^T | -R^T t]
-    double Di[12];
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j) Di[i * 4 + j] = D[j * 4 + i];
-        Di[i * 4 + 3] = -((D[0 * 4 + i] * D[3] + D[1 * 4 + i] * D[7]) + D[2 * 4 + i] * D[11]);
+    __syncwarp();
+    if (!st->failed && lane < 12) fs->dt[lane] = D[lane];
+    if (!ok) return;
+    if (lane < 12) {
+        // DT^-1 = [R^T | -R^T t]
+        const int i = lane / 4, j = lane % 4;
+        Di[lane] = j < 3 ? D[j * 4 + i] : -((D[0 * 4 + i] * D[3] + D[1 * 4 + i] * D[7]) + D[2 * 4 + i] * D[11]);
+        A[lane] = fs->Tcm[lane];
     }
-    double o[12];
-    const double *A = fs->Tcm;
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j)
-            o[i * 4 + j] = (A[i * 4 + 0] * Di[0 * 4 + j] + A[i * 4 + 1] * Di[1 * 4 + j]) + A[i * 4 + 2] * Di[2 * 4 + j];
-        o[i * 4 + 3] = ((A[i * 4 + 0] * Di[3] + A[i * 4 + 1] * Di[7]) + A[i * 4 + 2] * Di[11]) + A[i * 4 + 3];
+    __syncwarp();
+    if (lane < 12) {
+        const int i = lane / 4, j = lane % 4;
+        double o = (A[i * 4 + 0] * Di[0 * 4 + j] + A[i * 4 + 1] * Di[1 * 4 + j]) + A[i * 4 + 2] * Di[2 * 4 + j];
+        if (j == 3) o += A[i * 4 + 3];
+        fs->Tcm[lane] = o;
     }
-    for (int i = 0; i < 12; ++i) fs->Tcm[i] = o[i];
-    publish_pose(fs);
-    fs->skip = 0;
-    fs->status = YAS_OK;
-    hdr->n_visible = 0;
+    __syncwarp();
+    publish_pose(fs, lane);
+    if (lane == 0) {
+        fs->skip = 0;
+        fs->status = YAS_OK;
+        hdr->n_visible = 0;
+    }
 }
 
 }  // namespace yas

@@ -56,7 +56,8 @@ struct PassArgs {
     const float4 *cur_vmap;
     const float4 *cur_nmap;
     float4 *res4;
-    double *partial;
+    float *partial;
+    float *grow;
     unsigned *counter;
     GNState *st;
     double Kd[kMaxLevels][4];
@@ -79,250 +80,393 @@ __device__ __forceinline__ float warp_transpose_reduce(float v[32]) {
     return v[0];
 }
 
-// CTA reduction of 32 values + last-CTA FP64 combine.  Returns true in the last
-// CTA, where tot[0..31] (shared) holds the grid totals.
-__device__ __forceinline__ bool grid_reduce32(float v[32], double *partial, unsigned *counter,
+// Error-free transformation of a + b (Knuth's TwoSum): a + b == s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// CTA reduction of 32 values, then the grid totals by a two-level tree of
+// "last CTA to finish" reducers (ticket counters, nobody waits):
+//   * per CTA: warp transpose reduction and an 8-way cross-warp sum
+//     (pairwise, FP32) give one FP32 row per CTA;
+//   * per group of kGroup CTAs: the group's last CTA folds its rows with
+//     compensated FP32 (TwoSum) into a (hi, lo) row;
+//   * grid: the last group reducer folds the group rows the same way in
+//     eight interleaved subsets and adds the eight subset sums in FP64.
+// Every level is one batch of independent loads, and the order is fixed, so
+// results are reproducible.  Returns true in the final CTA, where tot[0..31]
+// (shared) holds the totals.  counters[0] is the grid ticket, counters[1+g]
+// the ticket of group g; each is reset by the CTA that consumes it.
+constexpr unsigned kGroup = 32;
+
+__device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float *grow, unsigned *counters,
                                               double *tot) {
-    __shared__ float wsum[kTrackThreads / 32][32];
-    __shared__ double gsum[kTrackThreads / 32][32];
-    __shared__ bool last;
+    constexpr unsigned S = kTrackThreads / 32;  // subsets (= warps)
+    __shared__ float wsum[S][32];
+    __shared__ float lsum[S][32];
+    __shared__ double dsum[S][32];
+    __shared__ bool flag;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const unsigned c = threadIdx.x & 31, sub = threadIdx.x >> 5;
     float r = warp_transpose_reduce(v);
     wsum[warp][lane] = r;
     __syncthreads();
     if (threadIdx.x < 32) {
         float s = 0.0f;
 #pragma unroll
-        for (int w = 0; w < kTrackThreads / 32; ++w) s += wsum[w][threadIdx.x];
-        partial[blockIdx.x * 32 + threadIdx.x] = (double)s;
+        for (unsigned w = 0; w < S; ++w) s += wsum[w][threadIdx.x];
+        partial[blockIdx.x * 32 + threadIdx.x] = s;
         __threadfence();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned ticket = atomicAdd(counter, 1u);
-        last = (ticket == gridDim.x - 1);
+    const unsigned g = blockIdx.x / kGroup;
+    const unsigned g0 = g * kGroup;
+    const unsigned gsize = min(kGroup, gridDim.x - g0);
+    const unsigned ngroups = (gridDim.x + kGroup - 1) / kGroup;
+    if (threadIdx.x == 0) flag = (atomicAdd(&counters[1 + g], 1u) == gsize - 1);
+    __syncthreads();
+    if (!flag) return false;
+    __threadfence();
+    {  // group level: subset `sub` folds rows g0 + sub + S*q
+        float h = 0.0f, l = 0.0f, x[kGroup / S];
+#pragma unroll
+        for (unsigned q = 0; q < kGroup / S; ++q) {
+            const unsigned row = sub + S * q;
+            x[q] = row < gsize ? __ldcg(partial + (g0 + row) * 32 + c) : 0.0f;
+        }
+#pragma unroll
+        for (unsigned q = 0; q < kGroup / S; ++q) {
+            float s, e;
+            two_sum(h, x[q], s, e);
+            h = s;
+            l += e;
+        }
+        wsum[sub][c] = h;
+        lsum[sub][c] = l;
     }
     __syncthreads();
-    if (!last) return false;
+    if (threadIdx.x < 32) {
+        float h = wsum[0][c], l = lsum[0][c];
+#pragma unroll
+        for (unsigned k = 1; k < S; ++k) {
+            float s, e;
+            two_sum(h, wsum[k][c], s, e);
+            h = s;
+            l += e + lsum[k][c];
+        }
+        grow[g * 64 + c] = h;
+        grow[g * 64 + 32 + c] = l;
+        __threadfence();
+    }
+    if (threadIdx.x == 0) counters[1 + g] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) flag = (atomicAdd(&counters[0], 1u) == ngroups - 1);
+    __syncthreads();
+    if (!flag) return false;
     __threadfence();
-    {
-        const unsigned c = threadIdx.x & 31, g = threadIdx.x >> 5;
-        double acc = 0.0;
-        for (unsigned b = g; b < gridDim.x; b += kTrackThreads / 32) acc += __ldcg(partial + b * 32 + c);
-        gsum[g][c] = acc;
+    {  // grid level: subset `sub` folds group rows sub, sub + S, ...
+        float h = 0.0f, l = 0.0f;
+        for (unsigned row = sub; row < ngroups; row += 2 * S) {
+            const float xh0 = __ldcg(grow + row * 64 + c), xl0 = __ldcg(grow + row * 64 + 32 + c);
+            const bool two = row + S < ngroups;
+            const float xh1 = two ? __ldcg(grow + (row + S) * 64 + c) : 0.0f;
+            const float xl1 = two ? __ldcg(grow + (row + S) * 64 + 32 + c) : 0.0f;
+            float s, e;
+            two_sum(h, xh0, s, e);
+            h = s;
+            l += e + xl0;
+            two_sum(h, xh1, s, e);
+            h = s;
+            l += e + xl1;
+        }
+        dsum[sub][c] = (double)h + (double)l;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
         double s = 0.0;
 #pragma unroll
-        for (int g = 0; g < kTrackThreads / 32; ++g) s += gsum[g][threadIdx.x];
+        for (unsigned k = 0; k < S; ++k) s += dsum[k][threadIdx.x];
         tot[threadIdx.x] = s;
     }
-    if (threadIdx.x == 0) *counter = 0u;
+    if (threadIdx.x == 0) counters[0] = 0u;
     __syncthreads();
     return true;
 }
 
 // ---------------------------------------------------------------- FP64 algebra
-// LDL^T with diagonal pivoting (largest remaining diagonal, left-looking) and
-// a pseudo-inverse of D (|d| <= 1/DBL_MAX -> 0): the algorithm of Eigen 3's LDLT.
-__device__ void ldlt_solve6(const double *Ain, const double *bin, double *x) {
-    double A[36];
-    int tr[6];
-    for (int i = 0; i < 36; ++i) A[i] = Ain[i];
-    for (int k = 0; k < 6; ++k) {
-        int p = k;
-        double best = fabs(A[k * 6 + k]);
-        for (int i = k + 1; i < 6; ++i)
-            if (fabs(A[i * 6 + i]) > best) {
-                best = fabs(A[i * 6 + i]);
-                p = i;
-            }
-        tr[k] = p;
-        if (p != k) {
-            for (int j = 0; j < 6; ++j) {
-                double t = A[k * 6 + j];
-                A[k * 6 + j] = A[p * 6 + j];
-                A[p * 6 + j] = t;
-            }
-            for (int i = 0; i < 6; ++i) {
-                double t = A[i * 6 + k];
-                A[i * 6 + k] = A[i * 6 + p];
-                A[i * 6 + p] = t;
-            }
-        }
-        double temp[6];
-        if (k > 0) {
-            for (int j = 0; j < k; ++j) temp[j] = A[j * 6 + j] * A[k * 6 + j];
-            double s = 0.0;
-            for (int j = 0; j < k; ++j) s += A[k * 6 + j] * temp[j];
-            A[k * 6 + k] -= s;
-            for (int i = k + 1; i < 6; ++i) {
-                double t = 0.0;
-                for (int j = 0; j < k; ++j) t += A[i * 6 + j] * temp[j];
-                A[i * 6 + k] -= t;
-            }
-        }
-        const double d = A[k * 6 + k];
-        const bool valid = fabs(d) > 0.0;
-        if (k == 0 && !valid) {
-            // whole diagonal zero (or NaN): identity transpositions, solve as is
-            for (int j = 0; j < 6; ++j) tr[j] = j;
-            break;
-        }
-        if (valid)
-            for (int i = k + 1; i < 6; ++i) A[i * 6 + k] /= d;
-    }
-    double y[6];
-    for (int i = 0; i < 6; ++i) y[i] = bin[i];
-    for (int k = 0; k < 6; ++k) {
-        double t = y[k];
-        y[k] = y[tr[k]];
-        y[tr[k]] = t;
-    }
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < i; ++j) y[i] -= A[i * 6 + j] * y[j];
-    const double tol = 1.0 / DBL_MAX;
-    for (int i = 0; i < 6; ++i) y[i] = fabs(A[i * 6 + i]) > tol ? y[i] / A[i * 6 + i] : 0.0;
-    for (int i = 5; i >= 0; --i)
-        for (int j = i + 1; j < 6; ++j) y[i] -= A[j * 6 + i] * y[j];
-    for (int k = 5; k >= 0; --k) {
-        double t = y[k];
-        y[k] = y[tr[k]];
-        y[tr[k]] = t;
-    }
-    for (int i = 0; i < 6; ++i) x[i] = y[i];
+// FP64 on GB300 issues at a small fraction of the FP32 rate with a long
+// dependent latency, and an IEEE FP64 division is a multi-step sequence; the
+// solve therefore uses reciprocals from an FP32 seed refined by two Newton
+// steps in FP64 (relative error below 2^-52, i.e. within an ulp of 1/d) and
+// polynomial series instead of divisions wherever the argument is small.
+__device__ __forceinline__ double drcp(double d) {
+    const double ad = fabs(d);
+    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+    double r = (double)__frcp_rn((float)d);
+    r = fma(r, fma(-d, r, 1.0), r);
+    r = fma(r, fma(-d, r, 1.0), r);
+    return r;
 }
 
-// SE(3) exponential of (upsilon, omega): R = Rodrigues(omega),
-// t = V upsilon, V = I + (1-cos)/th^2 W + (th - sin)/th^3 W^2 (series below 1e-4).
-__device__ void se3_exp(const double *xi, double *T) {
-    const double wx = xi[3], wy = xi[4], wz = xi[5];
-    const double th2 = wx * wx + wy * wy + wz * wz;
-    double A, B, C;  // sin/th, (1-cos)/th^2, (th-sin)/th^3
-    if (th2 < 1e-8) {
-        A = 1.0 - th2 / 6.0 + th2 * th2 / 120.0;
-        B = 0.5 - th2 / 24.0 + th2 * th2 / 720.0;
-        C = 1.0 / 6.0 - th2 / 120.0 + th2 * th2 / 5040.0;
-    } else {
-        const double th = sqrt(th2);
-        double s, c;
-        sincos(th, &s, &c);
-        A = s / th;
-        B = (1.0 - c) / th2;
-        C = (th - s) / (th2 * th);
-    }
-    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
-    double W2[9];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            double s = 0;
-            for (int k = 0; k < 3; ++k) s += W[i * 3 + k] * W[k * 3 + j];
-            W2[i * 3 + j] = s;
-        }
-    double R[9], V[9];
-    for (int i = 0; i < 9; ++i) {
-        const double I = (i % 4 == 0) ? 1.0 : 0.0;
-        R[i] = I + A * W[i] + B * W2[i];
-        V[i] = I + B * W[i] + C * W2[i];
-    }
-    for (int i = 0; i < 3; ++i) {
-        T[i * 4 + 0] = R[i * 3 + 0];
-        T[i * 4 + 1] = R[i * 3 + 1];
-        T[i * 4 + 2] = R[i * 3 + 2];
-        T[i * 4 + 3] = V[i * 3 + 0] * xi[0] + V[i * 3 + 1] * xi[1] + V[i * 3 + 2] * xi[2];
-    }
-}
-
-// T (row-major 3x4) = A * B
-__device__ void pose_mul34(const double *A, const double *B, double *T) {
-    double o[12];
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j)
-            o[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j] + A[i * 4 + 2] * B[2 * 4 + j];
-        o[i * 4 + 3] = A[i * 4 + 0] * B[3] + A[i * 4 + 1] * B[7] + A[i * 4 + 2] * B[11] + A[i * 4 + 3];
-    }
-    for (int i = 0; i < 12; ++i) T[i] = o[i];
-}
-
-// Float copies of the estimate and R*K_l^-1 for every level.
+// Float copy of the estimate read by the pixel passes.
 __device__ void publish_estimate(GNState *st, const double Kd[kMaxLevels][4], int L) {
+    (void)Kd;
+    (void)L;
     const double *E = st->est;
     for (int i = 0; i < 12; ++i) st->Tf[i] = (float)E[i];
-    for (int l = 0; l < L; ++l) {
-        const double fx = Kd[l][0], fy = Kd[l][1], cx = Kd[l][2], cy = Kd[l][3];
-        for (int i = 0; i < 3; ++i) {
-            const double r0 = E[i * 4 + 0], r1 = E[i * 4 + 1], r2 = E[i * 4 + 2];
-            st->RKinv[l][i * 3 + 0] = (float)(r0 / fx);
-            st->RKinv[l][i * 3 + 1] = (float)(r1 / fy);
-            st->RKinv[l][i * 3 + 2] = (float)(-r0 * cx / fx - r1 * cy / fy + r2);
-        }
+}
+
+// R * K_l^-1 for TransformReferencePoint (ImageProc.cu:86-101), formed in FP32
+// from the FP32 estimate by each CTA (the reference forms it in FP64 and
+// rounds it to FP32; the two differ by an ulp).
+__device__ __forceinline__ void make_rkinv(const float *T, const LevelCam &c, float *RK) {
+    const float cxi = c.cx * c.invfx, cyi = c.cy * c.invfy;
+    for (int i = 0; i < 3; ++i) {
+        RK[i * 3 + 0] = T[i * 4 + 0] * c.invfx;
+        RK[i * 3 + 1] = T[i * 4 + 1] * c.invfy;
+        RK[i * 3 + 2] = T[i * 4 + 2] - T[i * 4 + 0] * cxi - T[i * 4 + 1] * cyi;
     }
 }
 
-__device__ void unpack_system(const double *v, double *H, double *b, double sH, double sb, bool add) {
-    int k = 0;
-    for (int i = 0; i < 6; ++i)
-        for (int j = i; j < 7; ++j) {
-            const double val = v[k++];
-            if (j == 6) {
-                b[i] = (add ? b[i] : 0.0) + sb * val;
-            } else {
-                const double h = (add ? H[i * 6 + j] : 0.0) + sH * val;
-                H[i * 6 + j] = h;
-                H[j * 6 + i] = h;
-            }
-        }
-}
+// Packed index k of the 28 products of [J | r]: rows i, columns j >= i
+// (RankUpdateHessian<6,7>, TrackingUtils.h:45-58).
+__constant__ signed char c_pack_i[27] = {0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 5, 5};
+// Taylor coefficients (in th^2) of sin(th)/th, (1-cos th)/th^2, (th-sin th)/th^3.
+__constant__ double c_exp_poly[3][5] = {
+    {1.0, -1.0 / 6.0, 1.0 / 120.0, -1.0 / 5040.0, 1.0 / 362880.0},
+    {0.5, -1.0 / 24.0, 1.0 / 720.0, -1.0 / 40320.0, 1.0 / 3628800.0},
+    {1.0 / 6.0, -1.0 / 120.0, 1.0 / 5040.0, -1.0 / 362880.0, 1.0 / 39916800.0}};
+__constant__ signed char c_pack_j[27] = {0, 1, 2, 3, 4, 5, 6, 1, 2, 3, 4, 5, 6, 2, 3, 4, 5, 6, 3, 4, 5, 6, 4, 5, 6, 5, 6};
 
-// Thread 0 of the last CTA of the final pass of an iteration.
-__device__ void gn_solve(const PassArgs &a) {
+// The solve of one Gauss-Newton iteration, executed by the 32 lanes of warp 0
+// of the final CTA (GetTransform's loop body, RGBDTracking.cu:184-207):
+//   H = H_rgb + 100 H_icp, b = b_rgb + 10 b_icp (RGBDTracking.cu:543-544);
+//   error = sqrt(residualSum) / (numResidual + 6), in FP32 as the reference;
+//   update = LDLT(H).solve(b) in FP64: LDL^T with diagonal pivoting (largest
+//   remaining diagonal, left-looking), pseudo-inverse of D (|d| <= 1/DBL_MAX
+//   -> 0), identity transpositions if the first pivot is zero (Eigen 3's LDLT);
+//   NaN in update(0): the iteration fails and the result is the identity;
+//   estimate = exp(update) * estimate (SE(3) exponential, FP64);
+//   the kept estimate is the one after an update whose error beat the level's.
+// Each FP64 warp instruction occupies GB300's FP64 pipe for the same time with
+// one or 32 active lanes, so the solve spreads every independent FP64 product
+// over lanes: the system is assembled by 27 lanes, the factorisation updates
+// rows in parallel, the substitutions go column by column over rows, and the
+// exponential and pose product use one lane per matrix entry.
+__device__ __noinline__ void gn_solve_warp(const PassArgs &a) {
+    __shared__ double M[36], y[6], tmp[6], bc[3], E[12], est[12], W[9], W2[9];
+    __shared__ int tr[6], brk, fail;
+    __shared__ double inv_piv;
     GNState *st = a.st;
-    double H[36], b[6];
-    double residualSum, numResidual;
+    const int lane = (int)(threadIdx.x & 31);
     const double *A = st->a_sums, *B = st->b_sums;
-    if (a.mode == YAS_TRACK_RGBD) {
-        unpack_system(B, H, b, 1.0, 1.0, false);
-        unpack_system(A, H, b, 100.0, 10.0, true);
-        residualSum = (double)(float)A[27];
-        numResidual = (double)(float)A[29];
-    } else if (a.mode == YAS_TRACK_RGB) {
-        unpack_system(B, H, b, 1.0, 1.0, false);
-        residualSum = (double)(float)B[27];
-        numResidual = (double)(float)A[29];
-    } else {
-        unpack_system(A, H, b, 1.0, 1.0, false);
-        residualSum = (double)(float)A[27];
-        numResidual = (double)(float)A[28];
+    // ---- assemble H and b
+    if (lane < 27) {
+        const int i = c_pack_i[lane], j = c_pack_j[lane];
+        double v, vb;
+        if (a.mode == YAS_TRACK_RGBD) {
+            v = fma(100.0, A[lane], B[lane]);
+            vb = fma(10.0, A[lane], B[lane]);
+        } else if (a.mode == YAS_TRACK_RGB) {
+            v = vb = B[lane];
+        } else {
+            v = vb = A[lane];
+        }
+        if (j == 6) {
+            y[i] = vb;
+        } else {
+            M[i * 6 + j] = v;
+            M[j * 6 + i] = v;
+        }
     }
-    for (int i = 0; i < 36; ++i) st->H[i] = H[i];
-    for (int i = 0; i < 6; ++i) st->b[i] = b[i];
-    st->stats[0] = residualSum;
-    st->stats[1] = numResidual;
-    st->stats[2] = st->huber_th;
-    st->stats[3] = A[28];
+    __syncwarp();
+    const double residualSum = (double)(float)(a.mode == YAS_TRACK_RGB ? B[27] : A[27]);
+    const double numResidual = (double)(float)(a.mode == YAS_TRACK_ICP ? A[28] : A[29]);
+    if (lane < 36) st->H[lane] = M[lane];
+    if (lane < 6) st->b[lane] = y[lane];
+    if (lane == 0) {
+        st->stats[0] = residualSum;
+        st->stats[1] = numResidual;
+        st->stats[2] = st->huber_th;
+        st->stats[3] = A[28];
+        brk = 0;
+        fail = 0;
+    }
+    if (lane < 4) st->H[32 + lane] = M[32 + lane];
+    __syncwarp();
     if (a.no_update) return;
     const float error = sqrtf((float)residualSum) / ((float)numResidual + 6.0f);
-    double upd[6];
-    ldlt_solve6(H, b, upd);
-    for (int i = 0; i < 6; ++i) st->last_update[i] = upd[i];
-    if (isnan(upd[0])) {
-        st->failed = 1;
-        for (int i = 0; i < 12; ++i) st->best[i] = (i % 5 == 0) ? 1.0 : 0.0;
-        return;
+    // ---- LDL^T with diagonal pivoting
+    __shared__ double inv_d[6];
+    __shared__ int valid_d[6];
+    for (int k = 0; k < 6; ++k) {
+        if (lane == 0) {
+            // largest |diagonal| among rows k..5, first one on ties, a NaN never
+            // wins (every comparison with it is false): non-negative IEEE
+            // doubles order like their bit patterns, so the search uses integers
+            auto key = [](double v) -> long long {
+                const double a = fabs(v);
+                return isnan(v) ? -1LL : __double_as_longlong(a);
+            };
+            int p = k;
+            long long best = key(M[k * 7]);
+            if (best >= 0)
+                for (int i = k + 1; i < 6; ++i) {
+                    const long long ki = key(M[i * 7]);
+                    if (ki > best) {
+                        best = ki;
+                        p = i;
+                    }
+                }
+            tr[k] = p;
+        }
+        __syncwarp();
+        const int p = tr[k];
+        if (p != k) {
+            if (lane < 6) {
+                const double t = M[k * 6 + lane];
+                M[k * 6 + lane] = M[p * 6 + lane];
+                M[p * 6 + lane] = t;
+            }
+            __syncwarp();
+            if (lane < 6) {
+                const double t = M[lane * 6 + k];
+                M[lane * 6 + k] = M[lane * 6 + p];
+                M[lane * 6 + p] = t;
+            }
+            __syncwarp();
+        }
+        if (k > 0) {
+            if (lane < k) tmp[lane] = M[lane * 7] * M[k * 6 + lane];
+            __syncwarp();
+            if (lane >= k && lane < 6) {
+                double s = 0.0;
+                for (int j = 0; j < k; ++j) s = fma(M[lane * 6 + j], tmp[j], s);
+                M[lane * 6 + k] -= s;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            const double d = M[k * 7];
+            const bool valid = fabs(d) > 0.0;
+            if (k == 0 && !valid) {
+                for (int j = 0; j < 6; ++j) tr[j] = j;
+                brk = 1;
+            }
+            valid_d[k] = valid;
+            inv_d[k] = valid ? drcp(d) : 0.0;
+        }
+        __syncwarp();
+        if (brk) break;
+        if (lane > k && lane < 6 && valid_d[k]) M[lane * 6 + k] *= inv_d[k];
+        __syncwarp();
     }
-    double E[12];
-    se3_exp(upd, E);
-    pose_mul34(E, st->est, st->est);
-    if (a.first_of_level) st->last_error = (double)FLT_MAX;
-    if ((double)error < st->last_error) {
-        for (int i = 0; i < 12; ++i) st->best[i] = st->est[i];
-        st->last_error = (double)error;
-        st->n_success++;
+    // ---- y = P b; L y' = y; D y'' = y'; L^T x = y''; x = P^T x
+    if (lane == 0)
+        for (int k = 0; k < 6; ++k) {
+            const double t = y[k];
+            y[k] = y[tr[k]];
+            y[tr[k]] = t;
+        }
+    __syncwarp();
+    for (int j = 0; j < 5; ++j) {
+        if (lane > j && lane < 6) y[lane] = fma(-M[lane * 6 + j], y[j], y[lane]);
+        __syncwarp();
     }
-    st->n_iter++;
-    st->level_of_last = a.level;
-    publish_estimate(st, a.Kd, a.L);
+    if (lane < 6) {
+        // pseudo-inverse of D: the pivots' reciprocals when factorised; after a
+        // zero first pivot the diagonal is used as it is
+        const double d = M[lane * 7];
+        const double inv = (!brk && valid_d[lane]) ? inv_d[lane] : drcp(d);
+        y[lane] = fabs(d) > 1.0 / DBL_MAX ? y[lane] * inv : 0.0;
+    }
+    __syncwarp();
+    for (int j = 5; j > 0; --j) {
+        if (lane < j) y[lane] = fma(-M[j * 6 + lane], y[j], y[lane]);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        for (int k = 5; k >= 0; --k) {
+            const double t = y[k];
+            y[k] = y[tr[k]];
+            y[tr[k]] = t;
+        }
+        for (int i = 0; i < 6; ++i) st->last_update[i] = y[i];
+        if (isnan(y[0])) {
+            st->failed = 1;
+            for (int i = 0; i < 12; ++i) st->best[i] = (i % 5 == 0) ? 1.0 : 0.0;
+            fail = 1;
+        }
+    }
+    __syncwarp();
+    if (fail) return;
+    // ---- SE(3) exponential: R = I + A W + B W^2, V = I + B W + C W^2, t = V upsilon
+    const double wx = y[3], wy = y[4], wz = y[5];
+    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
+    if (lane < 3) {
+        double c;
+        if (th2 < 1e-2) {
+            // Taylor series in th^2 to the th^8 term (truncation below 3e-18);
+            // lane 0: sin/th, lane 1: (1-cos)/th^2, lane 2: (th-sin)/th^3
+            const double t = th2;
+            c = fma(t, fma(t, fma(t, fma(t, c_exp_poly[lane][4], c_exp_poly[lane][3]), c_exp_poly[lane][2]),
+                           c_exp_poly[lane][1]),
+                    c_exp_poly[lane][0]);
+        } else {
+            const double th = sqrt(th2);
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            c = lane == 0 ? sn / th : (lane == 1 ? (1.0 - cs) / th2 : (th - sn) / (th2 * th));
+        }
+        bc[lane] = c;
+    }
+    if (lane < 9) {
+        const double Wm[9] = {0.0, -wz, wy, wz, 0.0, -wx, -wy, wx, 0.0};
+        W[lane] = Wm[lane];
+    }
+    if (lane < 12) est[lane] = st->est[lane];
+    __syncwarp();
+    if (lane < 9) {
+        const int i = lane / 3, j = lane % 3;
+        W2[lane] = fma(W[i * 3 + 0], W[0 * 3 + j], fma(W[i * 3 + 1], W[1 * 3 + j], W[i * 3 + 2] * W[2 * 3 + j]));
+    }
+    __syncwarp();
+    if (lane < 9) {
+        const double I = (lane % 4 == 0) ? 1.0 : 0.0;
+        const int i = lane / 3, j = lane % 3;
+        E[i * 4 + j] = fma(bc[0], W[lane], fma(bc[1], W2[lane], I));
+        // V row entries go to W2's slot after use: V = I + B W + C W^2
+        W2[lane] = fma(bc[1], W[lane], fma(bc[2], W2[lane], I));
+    }
+    __syncwarp();
+    if (lane < 3) E[lane * 4 + 3] = fma(W2[lane * 3 + 0], y[0], fma(W2[lane * 3 + 1], y[1], W2[lane * 3 + 2] * y[2]));
+    __syncwarp();
+    // ---- estimate = E * estimate
+    double o = 0.0;
+    if (lane < 12) {
+        const int i = lane / 4, j = lane % 4;
+        o = fma(E[i * 4 + 0], est[0 * 4 + j], fma(E[i * 4 + 1], est[1 * 4 + j], E[i * 4 + 2] * est[2 * 4 + j]));
+        if (j == 3) o += E[i * 4 + 3];
+        st->est[lane] = o;
+        st->Tf[lane] = (float)o;
+    }
+    __syncwarp();
+    // ---- acceptance on the error measured before the update
+    __shared__ int accept;
+    if (lane == 0) {
+        if (a.first_of_level) st->last_error = (double)FLT_MAX;
+        accept = (double)error < st->last_error;
+        if (accept) {
+            st->last_error = (double)error;
+            st->n_success++;
+        }
+        st->n_iter++;
+        st->level_of_last = a.level;
+    }
+    __syncwarp();
+    if (accept && lane < 12) st->best[lane] = o;
 }
 
 // ---------------------------------------------------------------- pixel math
@@ -344,13 +488,14 @@ __device__ __forceinline__ float bilinear(const float *__restrict__ m, int w, fl
            (__ldg(r1) * (1.0f - cx) + __ldg(r1 + 1) * cx) * cy;
 }
 
-__global__ void __launch_bounds__(kTrackThreads) gn_pass_a(PassArgs a) {
+__global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
     GNState *st = a.st;
     if (*(volatile int *)&st->failed) return;
     __shared__ float sT[12], sRK[9];
     __shared__ double tot[32];
     if (threadIdx.x < 12) sT[threadIdx.x] = st->Tf[threadIdx.x];
-    if (threadIdx.x < 9) sRK[threadIdx.x] = st->RKinv[a.level][threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) make_rkinv(sT, a.c, sRK);
     __syncthreads();
     const LevelCam c = a.c;
     const int n = c.w * c.h;
@@ -426,25 +571,35 @@ __global__ void __launch_bounds__(kTrackThreads) gn_pass_a(PassArgs a) {
             }
         }
     }
-    if (!grid_reduce32(acc, a.partial, a.counter, tot)) return;
+    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
     if (threadIdx.x < 32) st->a_sums[threadIdx.x] = tot[threadIdx.x];
+    __syncthreads();
     if (threadIdx.x == 0) {
-        // stddev of the photometric residuals (two-pass variance restated as
-        // sum r^2 - (sum r)^2 / n in FP64), Huber threshold 4.685 * stddev.
+        // Huber threshold 4.685 * stddev of the photometric residuals, in FP32
+        // as the reference (RGBDTracking.cu:259-278): mean = sum r / n, then
+        // sum (r - mean)^2 = sum r^2 - 2 mean sum r + n mean^2 from the FP64
+        // totals (the reference's second pass over the residuals).
         const double nn = tot[29], s = tot[30], s2 = tot[31];
-        const double var = (s2 - s * s / nn) / (nn - 1.0);
-        st->huber_th = (float)(4.685 * sqrt(var));
-        if (a.mode == YAS_TRACK_ICP) gn_solve(a);
+        const float mean = (float)s / (float)nn;
+        const double md = (double)mean;
+        const double ss = fma(nn * md, md, fma(-2.0 * md, s, s2));
+        const float var = sqrtf((float)ss / ((float)nn - 1.0f));
+        st->huber_th = (float)(4.685 * (double)var);
+    }
+    if (a.mode == YAS_TRACK_ICP) {
+        __syncthreads();
+        if (threadIdx.x < 32) gn_solve_warp(a);
     }
 }
 
-__global__ void __launch_bounds__(kTrackThreads) gn_pass_b(PassArgs a) {
+__global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_b(PassArgs a) {
     GNState *st = a.st;
     if (*(volatile int *)&st->failed) return;
     __shared__ float sT[12], sRK[9];
     __shared__ double tot[32];
     if (threadIdx.x < 12) sT[threadIdx.x] = st->Tf[threadIdx.x];
-    if (threadIdx.x < 9) sRK[threadIdx.x] = st->RKinv[a.level][threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) make_rkinv(sT, a.c, sRK);
     __syncthreads();
     const float th = st->huber_th;
     const LevelCam c = a.c;
@@ -476,10 +631,10 @@ __global__ void __launch_bounds__(kTrackThreads) gn_pass_b(PassArgs a) {
                 for (int j = i; j < 7; ++j) acc[q++] += wt * row[i] * row[j];
         }
     }
-    if (!grid_reduce32(acc, a.partial, a.counter, tot)) return;
+    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
     if (threadIdx.x < 32) st->b_sums[threadIdx.x] = tot[threadIdx.x];
     __syncthreads();
-    if (threadIdx.x == 0) gn_solve(a);
+    if (threadIdx.x < 32) gn_solve_warp(a);
 }
 
 __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) {
@@ -536,12 +691,14 @@ static void launch_passes(yas_tracker *tr, int l, int first, int no_update, cuda
     PassArgs a = make_args(tr, l, first, no_update);
     const int g = pass_grid(tr->cam[l]);
     a.partial = tr->partialA;
+    a.grow = tr->growA;
     a.counter = tr->counters;
     if (tr->hook) tr->hook(tr->hook_ctx, 10 + l);
     gn_pass_a<<<g, kTrackThreads, 0, s>>>(a);
     if (tr->mode & YAS_TRACK_RGB) {
         a.partial = tr->partialB;
-        a.counter = tr->counters + 1;
+        a.grow = tr->growB;
+        a.counter = tr->counters + kMaxCtas / kGroup + 1;
         if (tr->hook) tr->hook(tr->hook_ctx, 20 + l);
         gn_pass_b<<<g, kTrackThreads, 0, s>>>(a);
     }
@@ -589,13 +746,15 @@ int tracker_alloc(yas_tracker *tr) {
         if (!tr->gx[l] || !tr->gy[l]) return YAS_ERR_OOM;
     }
     tr->res4 = (float4 *)grab((size_t)tr->w * tr->h * 16);
-    tr->partialA = (double *)grab((size_t)kMaxCtas * 32 * 8);
-    tr->partialB = (double *)grab((size_t)kMaxCtas * 32 * 8);
-    tr->counters = (unsigned *)grab(64);
+    tr->partialA = (float *)grab((size_t)kMaxCtas * 32 * 4);
+    tr->partialB = (float *)grab((size_t)kMaxCtas * 32 * 4);
+    tr->growA = (float *)grab((size_t)(kMaxCtas / kGroup) * 64 * 4);
+    tr->growB = (float *)grab((size_t)(kMaxCtas / kGroup) * 64 * 4);
+    tr->counters = (unsigned *)grab((size_t)2 * (kMaxCtas / kGroup + 1) * 4);
     tr->state = (GNState *)grab(sizeof(GNState));
     tr->staging_bytes = (size_t)tr->w * tr->h * 4;
     tr->staging = grab(tr->staging_bytes);
-    if (!tr->res4 || !tr->partialA || !tr->partialB || !tr->counters || !tr->state || !tr->staging)
+    if (!tr->res4 || !tr->partialA || !tr->partialB || !tr->growA || !tr->growB || !tr->counters || !tr->state || !tr->staging)
         return YAS_ERR_OOM;
     if (cudaMallocHost(&tr->state_host, sizeof(GNState)) != cudaSuccess) {
         cudaGetLastError();

@@ -8,9 +8,9 @@ namespace yas {
 
 constexpr int kMaxLevels = 5;
 constexpr int kRedWidth = 32;       // values reduced per CTA (padded)
-constexpr int kMaxCtas = 1024;      // partial-sum rows per pass
+constexpr int kMaxCtas = 8192;      // partial-sum rows per pass
 constexpr int kTrackThreads = 256;
-constexpr int kPixPerThread = 4;
+constexpr int kPixPerThread = 1;
 
 // Camera of one pyramid level: K / 2^l with K(2,2) = 1 (RGBDTracking.cu:16-26).
 struct LevelCam {
@@ -73,9 +73,11 @@ struct yas_tracker {
     float *gy[yas::kMaxLevels] = {nullptr};
     int cur = 0;  // current-frame set; the reference set is 1 - cur
     float4 *res4 = nullptr;       // per-pixel photometric residual (level-0 sized)
-    double *partialA = nullptr;   // kMaxCtas x 32
-    double *partialB = nullptr;   // kMaxCtas x 32
-    unsigned *counters = nullptr; // [0] pass A, [1] pass B
+    float *partialA = nullptr;    // kMaxCtas x 32 per-CTA rows
+    float *partialB = nullptr;    // kMaxCtas x 32
+    float *growA = nullptr;       // per-group (hi, lo) rows of pass A
+    float *growB = nullptr;       // per-group (hi, lo) rows of pass B
+    unsigned *counters = nullptr; // tickets: pass A grid + groups, then pass B grid + groups
     yas::GNState *state = nullptr;
     yas::GNState *state_host = nullptr;  // pinned
     void *staging = nullptr;             // host-input staging (w*h*4 bytes)
