@@ -221,6 +221,19 @@ void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const in
 }
 
 // ---------------------------------------------------------------- integration
+// Pixel index floor(((a / z) + c) + 0.5) with the IEEE quotient a / z, as the
+// canonical FP32 order defines it.  The quotient is first formed as a * (1/z)
+// with the correctly rounded reciprocal (within 2 ulp of a / z); only when the
+// resulting coordinate lies within 8 ulp of an integer, where the two could
+// round to different pixels, is the exact division evaluated.
+__device__ __forceinline__ int project_exact(float a, float z, float rz, float c) {
+    const float t = cadd(cadd(cmul(a, rz), c), 0.5f);
+    const float ft = floorf(t);
+    const float tol = 8.0f * fmaxf(fabsf(t), fabsf(t - c)) * 1.1920929e-7f;
+    if (fabsf(t) < 8.0e6f && t - ft > tol && ft + 1.0f - t > tol) return (int)ft;
+    return f2i_floor(cadd(cadd(cdiv(a, z), c), 0.5f));
+}
+
 // Each 128-thread group owns one block; thread t updates voxels 4t..4t+3
 // (z = t/16, y = (t/2)%8, x = 4*(t%2) .. +3), one 16-byte (or 32-byte) access.
 template <int FMT>
@@ -234,7 +247,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
     const Rigid32 Tinv = P->Tinv;
     const int t = threadIdx.x & 127;
     const int lz = t >> 4, ly = (t >> 1) & 7, lx0 = (t & 1) * 4;
-    const float vs = m.voxel_size, trunc = m.trunc, ntrunc = -m.trunc;
+    const float vs = m.voxel_size, inv_trunc = 1.0f / m.trunc, ntrunc = -m.trunc;
     V *vox = static_cast<V *>(m.voxels);
     for (unsigned j = blockIdx.x * 2 + (threadIdx.x >> 7); j < nvis; j += gridDim.x * 2) {
         const int b = m.visible[j];
@@ -263,21 +276,22 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
         for (int q = 0; q < 4; ++q) {
             const float wx = cmul((float)(bx * 8 + lx0 + q), vs);
             float3 pc = rigid_exact(Tinv, wx, wy, wz);
-            int u = f2i_floor(cadd(cadd(cdiv(cmul(cam.fx, pc.x), pc.z), cam.cx), 0.5f));
-            int vv = f2i_floor(cadd(cadd(cdiv(cmul(cam.fy, pc.y), pc.z), cam.cy), 0.5f));
+            const float rz = __frcp_rn(pc.z);
+            int u = project_exact(cmul(cam.fx, pc.x), pc.z, rz, cam.cx);
+            int vv = project_exact(cmul(cam.fy, pc.y), pc.z, rz, cam.cy);
             if (u < 0 || vv < 0 || u > cam.w - 1 || vv > cam.h - 1) continue;
             float dist = __ldg(depth + (size_t)vv * pitch + u);
             if (isnan(dist) || dist > m.depth_max || dist < m.depth_min) continue;
             float sdf = csub(dist, pc.z);
             if (sdf < ntrunc) continue;
-            sdf = fminf(1.0f, cdiv(sdf, trunc));
+            sdf = fminf(1.0f, sdf * inv_trunc);
             int w = IO::wt(v[q]);
             float ns;
             if (w == 0) {
                 ns = sdf;
                 w = 1;
             } else {
-                ns = (IO::sdf(v[q]) * (float)w + sdf) / (float)(w + 1);
+                ns = __fdividef(fmaf(IO::sdf(v[q]), (float)w, sdf), (float)(w + 1));
                 w = min(m.max_weight, w + 1);
             }
             v[q] = IO::make(ns, w);

@@ -196,19 +196,9 @@ __device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float
 }
 
 // ---------------------------------------------------------------- FP64 algebra
-// FP64 on GB300 issues at a small fraction of the FP32 rate with a long
-// dependent latency, and an IEEE FP64 division is a multi-step sequence; the
-// solve therefore uses reciprocals from an FP32 seed refined by two Newton
-// steps in FP64 (relative error below 2^-52, i.e. within an ulp of 1/d) and
-// polynomial series instead of divisions wherever the argument is small.
-__device__ __forceinline__ double drcp(double d) {
-    const double ad = fabs(d);
-    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
-    double r = (double)__frcp_rn((float)d);
-    r = fma(r, fma(-d, r, 1.0), r);
-    r = fma(r, fma(-d, r, 1.0), r);
-    return r;
-}
+// FP64 on GB300 has a dependent latency of about 65 cycles (16x FP32) and an
+// IEEE FP64 division is a multi-step sequence; the solve therefore avoids
+// divisions (FP32-seeded reciprocals, polynomial series for small angles).
 
 // Float copy of the estimate read by the pixel passes.
 __device__ void publish_estimate(GNState *st, const double Kd[kMaxLevels][4], int L) {
@@ -240,221 +230,232 @@ __constant__ double c_exp_poly[3][5] = {
     {1.0 / 6.0, -1.0 / 120.0, 1.0 / 5040.0, -1.0 / 362880.0, 1.0 / 39916800.0}};
 __constant__ signed char c_pack_j[27] = {0, 1, 2, 3, 4, 5, 6, 1, 2, 3, 4, 5, 6, 2, 3, 4, 5, 6, 3, 4, 5, 6, 4, 5, 6, 5, 6};
 
+// Reciprocal for the solve: FP32 seed and one Newton step in FP64 (relative
+// error below 2^-46, far under the ~1e-7 precision of the FP32-accumulated
+// system it is applied to).
+__device__ __forceinline__ double drcp1(double d) {
+    const double ad = fabs(d);
+    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+    const double r = (double)__frcp_rn((float)d);
+    return fma(r, fma(-d, r, 1.0), r);
+}
+
+__device__ __forceinline__ int pack_index(int r, int c) { return 7 * r - (r * (r - 1)) / 2 + c - r; }
+
 // The solve of one Gauss-Newton iteration, executed by the 32 lanes of warp 0
 // of the final CTA (GetTransform's loop body, RGBDTracking.cu:184-207):
 //   H = H_rgb + 100 H_icp, b = b_rgb + 10 b_icp (RGBDTracking.cu:543-544);
 //   error = sqrt(residualSum) / (numResidual + 6), in FP32 as the reference;
 //   update = LDLT(H).solve(b) in FP64: LDL^T with diagonal pivoting (largest
-//   remaining diagonal, left-looking), pseudo-inverse of D (|d| <= 1/DBL_MAX
-//   -> 0), identity transpositions if the first pivot is zero (Eigen 3's LDLT);
+//   remaining diagonal, first on ties, left-looking), pseudo-inverse of D
+//   (|d| <= 1/DBL_MAX -> 0), identity transpositions and no factorisation if
+//   the first pivot is zero (Eigen 3's LDLT);
 //   NaN in update(0): the iteration fails and the result is the identity;
 //   estimate = exp(update) * estimate (SE(3) exponential, FP64);
 //   the kept estimate is the one after an update whose error beat the level's.
-// Each FP64 warp instruction occupies GB300's FP64 pipe for the same time with
-// one or 32 active lanes, so the solve spreads every independent FP64 product
-// over lanes: the system is assembled by 27 lanes, the factorisation updates
-// rows in parallel, the substitutions go column by column over rows, and the
-// exponential and pose product use one lane per matrix entry.
+// GB300's dependent FP64 latency is ~65 cycles, so the solve keeps row i of H
+// in the registers of lane i, moves columns between lanes with shuffles, runs
+// every independent FP64 product on its own lane, and unrolls the
+// factorisation so that every register index is static.
 __device__ __noinline__ void gn_solve_warp(const PassArgs &a) {
-    __shared__ double M[36], y[6], tmp[6], bc[3], E[12], est[12], W[9], W2[9];
-    __shared__ int tr[6], brk, fail;
-    __shared__ double inv_piv;
+    __shared__ double Ls[36];
     GNState *st = a.st;
     const int lane = (int)(threadIdx.x & 31);
     const double *A = st->a_sums, *B = st->b_sums;
-    // ---- assemble H and b
-    if (lane < 27) {
-        const int i = c_pack_i[lane], j = c_pack_j[lane];
-        double v, vb;
-        if (a.mode == YAS_TRACK_RGBD) {
-            v = fma(100.0, A[lane], B[lane]);
-            vb = fma(10.0, A[lane], B[lane]);
-        } else if (a.mode == YAS_TRACK_RGB) {
-            v = vb = B[lane];
-        } else {
-            v = vb = A[lane];
-        }
-        if (j == 6) {
-            y[i] = vb;
-        } else {
-            M[i * 6 + j] = v;
-            M[j * 6 + i] = v;
+    const bool rowlane = lane < 6;
+    // ---- assemble row `lane` of H and b[lane]
+    double row[6], y = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        row[j] = 0.0;
+        if (rowlane) {
+            const int kk = pack_index(min(lane, j), max(lane, j));
+            row[j] = a.mode == YAS_TRACK_RGBD ? fma(100.0, A[kk], B[kk]) : (a.mode == YAS_TRACK_RGB ? B[kk] : A[kk]);
         }
     }
-    __syncwarp();
+    if (rowlane) {
+        const int kk = pack_index(lane, 6);
+        y = a.mode == YAS_TRACK_RGBD ? fma(10.0, A[kk], B[kk]) : (a.mode == YAS_TRACK_RGB ? B[kk] : A[kk]);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) st->H[lane * 6 + j] = row[j];
+        st->b[lane] = y;
+    }
     const double residualSum = (double)(float)(a.mode == YAS_TRACK_RGB ? B[27] : A[27]);
     const double numResidual = (double)(float)(a.mode == YAS_TRACK_ICP ? A[28] : A[29]);
-    if (lane < 36) st->H[lane] = M[lane];
-    if (lane < 6) st->b[lane] = y[lane];
     if (lane == 0) {
         st->stats[0] = residualSum;
         st->stats[1] = numResidual;
         st->stats[2] = st->huber_th;
         st->stats[3] = A[28];
-        brk = 0;
-        fail = 0;
     }
-    if (lane < 4) st->H[32 + lane] = M[32 + lane];
-    __syncwarp();
     if (a.no_update) return;
     const float error = sqrtf((float)residualSum) / ((float)numResidual + 6.0f);
     // ---- LDL^T with diagonal pivoting
-    __shared__ double inv_d[6];
-    __shared__ int valid_d[6];
+    double Dv[6];
+    int trk[6];
+    bool broke = false;
+#pragma unroll
     for (int k = 0; k < 6; ++k) {
-        if (lane == 0) {
-            // largest |diagonal| among rows k..5, first one on ties, a NaN never
-            // wins (every comparison with it is false): non-negative IEEE
-            // doubles order like their bit patterns, so the search uses integers
-            auto key = [](double v) -> long long {
-                const double a = fabs(v);
-                return isnan(v) ? -1LL : __double_as_longlong(a);
-            };
-            int p = k;
-            long long best = key(M[k * 7]);
-            if (best >= 0)
-                for (int i = k + 1; i < 6; ++i) {
-                    const long long ki = key(M[i * 7]);
-                    if (ki > best) {
-                        best = ki;
-                        p = i;
-                    }
+        Dv[k] = 0.0;
+        trk[k] = k;
+        if (broke) continue;
+        // pivot: largest |diagonal| over rows k..5, first one on ties; a NaN
+        // never wins (every comparison with it is false) and a NaN at row k
+        // keeps row k; non-negative doubles order like their bit patterns
+        double diag = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+            if (lane == q) diag = row[q];
+        long long key = (lane >= k && lane < 6) ? (isnan(diag) ? -1LL : __double_as_longlong(fabs(diag))) : -2LL;
+        const long long keyk = __shfl_sync(0xffffffffu, key, k);
+        int p = k;
+        if (keyk >= 0) {
+            long long bk = key;
+            int bl = lane;
+#pragma unroll
+            for (int off = 1; off < 8; off <<= 1) {
+                const long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
+                const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+                if (ok > bk || (ok == bk && ol < bl)) {
+                    bk = ok;
+                    bl = ol;
                 }
-            tr[k] = p;
+            }
+            p = __shfl_sync(0xffffffffu, bl, 0);
         }
-        __syncwarp();
-        const int p = tr[k];
+        trk[k] = p;
         if (p != k) {
-            if (lane < 6) {
-                const double t = M[k * 6 + lane];
-                M[k * 6 + lane] = M[p * 6 + lane];
-                M[p * 6 + lane] = t;
-            }
-            __syncwarp();
-            if (lane < 6) {
-                const double t = M[lane * 6 + k];
-                M[lane * 6 + k] = M[lane * 6 + p];
-                M[lane * 6 + p] = t;
-            }
-            __syncwarp();
+            // rows k and p change lanes, then every row swaps columns k and p
+            const int src = lane == k ? p : (lane == p ? k : lane);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) row[q] = __shfl_sync(0xffffffffu, row[q], src);
+#pragma unroll
+            for (int q = k + 1; q < 6; ++q)
+                if (q == p) {
+                    const double t = row[k];
+                    row[k] = row[q];
+                    row[q] = t;
+                }
         }
         if (k > 0) {
-            if (lane < k) tmp[lane] = M[lane * 7] * M[k * 6 + lane];
-            __syncwarp();
-            if (lane >= k && lane < 6) {
-                double s = 0.0;
-                for (int j = 0; j < k; ++j) s = fma(M[lane * 6 + j], tmp[j], s);
-                M[lane * 6 + k] -= s;
-            }
-            __syncwarp();
+            double tmp[6];
+#pragma unroll
+            for (int j = 0; j < k; ++j) tmp[j] = Dv[j] * __shfl_sync(0xffffffffu, row[j], k);
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < k; ++j) s = fma(row[j], tmp[j], s);
+            if (lane >= k) row[k] -= s;
         }
-        if (lane == 0) {
-            const double d = M[k * 7];
-            const bool valid = fabs(d) > 0.0;
-            if (k == 0 && !valid) {
-                for (int j = 0; j < 6; ++j) tr[j] = j;
-                brk = 1;
-            }
-            valid_d[k] = valid;
-            inv_d[k] = valid ? drcp(d) : 0.0;
+        const double d = __shfl_sync(0xffffffffu, row[k], k);
+        Dv[k] = d;
+        const bool valid = fabs(d) > 0.0;
+        if (k == 0 && !valid) {
+            broke = true;  // identity transpositions, the matrix is used as it is
+            continue;
         }
-        __syncwarp();
-        if (brk) break;
-        if (lane > k && lane < 6 && valid_d[k]) M[lane * 6 + k] *= inv_d[k];
-        __syncwarp();
+        if (valid && lane > k) row[k] *= drcp1(d);
     }
     // ---- y = P b; L y' = y; D y'' = y'; L^T x = y''; x = P^T x
-    if (lane == 0)
-        for (int k = 0; k < 6; ++k) {
-            const double t = y[k];
-            y[k] = y[tr[k]];
-            y[tr[k]] = t;
-        }
-    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int p = trk[k];
+        const int src = lane == k ? p : (lane == p ? k : lane);
+        y = __shfl_sync(0xffffffffu, y, src);
+    }
+#pragma unroll
     for (int j = 0; j < 5; ++j) {
-        if (lane > j && lane < 6) y[lane] = fma(-M[lane * 6 + j], y[j], y[lane]);
-        __syncwarp();
+        const double yj = __shfl_sync(0xffffffffu, y, j);
+        if (lane > j && rowlane) y = fma(-row[j], yj, y);
     }
-    if (lane < 6) {
-        // pseudo-inverse of D: the pivots' reciprocals when factorised; after a
-        // zero first pivot the diagonal is used as it is
-        const double d = M[lane * 7];
-        const double inv = (!brk && valid_d[lane]) ? inv_d[lane] : drcp(d);
-        y[lane] = fabs(d) > 1.0 / DBL_MAX ? y[lane] * inv : 0.0;
+    {
+        double dd = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+            if (lane == q) dd = row[q];
+        y = (rowlane && fabs(dd) > 1.0 / DBL_MAX) ? y * drcp1(dd) : 0.0;
+    }
+    if (rowlane) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) Ls[lane * 6 + q] = row[q];
     }
     __syncwarp();
+#pragma unroll
     for (int j = 5; j > 0; --j) {
-        if (lane < j) y[lane] = fma(-M[j * 6 + lane], y[j], y[lane]);
-        __syncwarp();
+        const double yj = __shfl_sync(0xffffffffu, y, j);
+        const double lji = rowlane ? Ls[j * 6 + lane] : 0.0;  // L(j, lane)
+        if (lane < j) y = fma(-lji, yj, y);
     }
-    if (lane == 0) {
-        for (int k = 5; k >= 0; --k) {
-            const double t = y[k];
-            y[k] = y[tr[k]];
-            y[tr[k]] = t;
-        }
-        for (int i = 0; i < 6; ++i) st->last_update[i] = y[i];
-        if (isnan(y[0])) {
-            st->failed = 1;
-            for (int i = 0; i < 12; ++i) st->best[i] = (i % 5 == 0) ? 1.0 : 0.0;
-            fail = 1;
-        }
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        const int p = trk[k];
+        const int src = lane == k ? p : (lane == p ? k : lane);
+        y = __shfl_sync(0xffffffffu, y, src);
     }
-    __syncwarp();
-    if (fail) return;
-    // ---- SE(3) exponential: R = I + A W + B W^2, V = I + B W + C W^2, t = V upsilon
-    const double wx = y[3], wy = y[4], wz = y[5];
+    double u[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) u[q] = __shfl_sync(0xffffffffu, y, q);
+    if (lane < 6) st->last_update[lane] = y;
+    if (isnan(u[0])) {
+        if (lane == 0) st->failed = 1;
+        if (lane < 12) st->best[lane] = (lane % 5 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    // ---- SE(3) exponential, one matrix entry per lane:
+    // R = I + A W + B W^2, t = V v, V = I + B W + C W^2, W = hat(w),
+    // W^2 = w w^T - th^2 I, W v = w x v
+    const double wx = u[3], wy = u[4], wz = u[5];
     const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
-    if (lane < 3) {
-        double c;
-        if (th2 < 1e-2) {
-            // Taylor series in th^2 to the th^8 term (truncation below 3e-18);
-            // lane 0: sin/th, lane 1: (1-cos)/th^2, lane 2: (th-sin)/th^3
-            const double t = th2;
-            c = fma(t, fma(t, fma(t, fma(t, c_exp_poly[lane][4], c_exp_poly[lane][3]), c_exp_poly[lane][2]),
-                           c_exp_poly[lane][1]),
-                    c_exp_poly[lane][0]);
-        } else {
-            const double th = sqrt(th2);
-            double sn, cs;
-            sincos(th, &sn, &cs);
-            c = lane == 0 ? sn / th : (lane == 1 ? (1.0 - cs) / th2 : (th - sn) / (th2 * th));
-        }
-        bc[lane] = c;
+    double cA, cB, cC;
+    if (th2 < 1e-2) {
+        // Taylor series in th^2 to the th^8 term (truncation below 3e-18)
+        cA = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[0][4], c_exp_poly[0][3]), c_exp_poly[0][2]), c_exp_poly[0][1]),
+                 c_exp_poly[0][0]);
+        cB = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[1][4], c_exp_poly[1][3]), c_exp_poly[1][2]), c_exp_poly[1][1]),
+                 c_exp_poly[1][0]);
+        cC = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[2][4], c_exp_poly[2][3]), c_exp_poly[2][2]), c_exp_poly[2][1]),
+                 c_exp_poly[2][0]);
+    } else {
+        const double th = sqrt(th2);
+        double sn, cs;
+        sincos(th, &sn, &cs);
+        cA = sn / th;
+        cB = (1.0 - cs) / th2;
+        cC = (th - sn) / (th2 * th);
     }
-    if (lane < 9) {
-        const double Wm[9] = {0.0, -wz, wy, wz, 0.0, -wx, -wy, wx, 0.0};
-        W[lane] = Wm[lane];
+    const double w[3] = {wx, wy, wz};
+    const int i = (lane < 12) ? lane / 4 : 0, jc = (lane < 12) ? lane % 4 : 0;
+    // row i of E: E(i,q) = d(i,q) + A W(i,q) + B (w_i w_q - d(i,q) th^2)
+    double Er[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double Wiq = (i == q) ? 0.0
+                                    : ((i == 0 && q == 1) ? -wz
+                                       : (i == 0 && q == 2) ? wy
+                                       : (i == 1 && q == 0) ? wz
+                                       : (i == 1 && q == 2) ? -wx
+                                       : (i == 2 && q == 0) ? -wy
+                                                            : wx);
+        const double dq = (i == q) ? 1.0 : 0.0;
+        Er[q] = fma(cA, Wiq, fma(cB, fma(w[i], w[q], -dq * th2), dq));
     }
-    if (lane < 12) est[lane] = st->est[lane];
-    __syncwarp();
-    if (lane < 9) {
-        const int i = lane / 3, j = lane % 3;
-        W2[lane] = fma(W[i * 3 + 0], W[0 * 3 + j], fma(W[i * 3 + 1], W[1 * 3 + j], W[i * 3 + 2] * W[2 * 3 + j]));
-    }
-    __syncwarp();
-    if (lane < 9) {
-        const double I = (lane % 4 == 0) ? 1.0 : 0.0;
-        const int i = lane / 3, j = lane % 3;
-        E[i * 4 + j] = fma(bc[0], W[lane], fma(bc[1], W2[lane], I));
-        // V row entries go to W2's slot after use: V = I + B W + C W^2
-        W2[lane] = fma(bc[1], W[lane], fma(bc[2], W2[lane], I));
-    }
-    __syncwarp();
-    if (lane < 3) E[lane * 4 + 3] = fma(W2[lane * 3 + 0], y[0], fma(W2[lane * 3 + 1], y[1], W2[lane * 3 + 2] * y[2]));
-    __syncwarp();
-    // ---- estimate = E * estimate
+    // t_i = v_i + B (w x v)_i + C (w_i (w . v) - th^2 v_i)
+    const double wxv[3] = {wy * u[2] - wz * u[1], wz * u[0] - wx * u[2], wx * u[1] - wy * u[0]};
+    const double wdv = fma(wx, u[0], fma(wy, u[1], wz * u[2]));
+    const double ti = fma(cB, wxv[i], fma(cC, fma(w[i], wdv, -th2 * u[i]), u[i]));
+    // ---- estimate = E * estimate, entry (i, jc) on lane i*4 + jc
     double o = 0.0;
     if (lane < 12) {
-        const int i = lane / 4, j = lane % 4;
-        o = fma(E[i * 4 + 0], est[0 * 4 + j], fma(E[i * 4 + 1], est[1 * 4 + j], E[i * 4 + 2] * est[2 * 4 + j]));
-        if (j == 3) o += E[i * 4 + 3];
+        const double e0 = st->est[0 * 4 + jc], e1 = st->est[1 * 4 + jc], e2 = st->est[2 * 4 + jc];
+        o = fma(Er[0], e0, fma(Er[1], e1, Er[2] * e2));
+        if (jc == 3) o += ti;
+    }
+    __syncwarp();
+    if (lane < 12) {
         st->est[lane] = o;
         st->Tf[lane] = (float)o;
     }
-    __syncwarp();
     // ---- acceptance on the error measured before the update
-    __shared__ int accept;
+    int accept = 0;
     if (lane == 0) {
         if (a.first_of_level) st->last_error = (double)FLT_MAX;
         accept = (double)error < st->last_error;
@@ -465,7 +466,7 @@ __device__ __noinline__ void gn_solve_warp(const PassArgs &a) {
         st->n_iter++;
         st->level_of_last = a.level;
     }
-    __syncwarp();
+    accept = __shfl_sync(0xffffffffu, accept, 0);
     if (accept && lane < 12) st->best[lane] = o;
 }
 
