@@ -222,6 +222,43 @@ YAS_API int yas_tracker_compute_step(yas_tracker *tr, int level, const yas_pose 
 YAS_API int yas_tracker_level_buffer(yas_tracker *tr, int level, int which, const void **dev_ptr,
                                      int *width, int *height, int *pitch_bytes);
 
+/* One pyramid level of the tracker's inputs, as device pointers to dense
+ * row-major images of width x height (no padding).  vmap/nmap are float4
+ * (x, y, z, w) with w > 0 for valid entries. */
+typedef struct yas_gn_level {
+    int width, height;
+    float fx, fy, cx, cy;       /* intrinsics of this level                   */
+    const float *ref_intensity; /* reference frame intensity                  */
+    const float *ref_inv_depth; /* reference frame inverse depth (0 = none)   */
+    const float *ref_vmap;      /* reference model vertices (float4)          */
+    const float *ref_nmap;      /* reference model normals (float4)           */
+    const float *cur_intensity; /* current frame intensity                    */
+    const float *cur_gx;        /* current frame intensity gradient x         */
+    const float *cur_gy;        /* current frame intensity gradient y         */
+    const float *cur_vmap;      /* current frame vertices (float4)            */
+    const float *cur_nmap;      /* current frame normals (float4)             */
+} yas_gn_level;
+
+/* No counterpart in the reference.  One Gauss-Newton linearisation at pose T
+ * (what yas_tracker_compute_step computes: H, b and the statistics) for
+ * callers that must not allocate device memory: a host that owns the whole
+ * device-memory budget of the process, or code that runs where an allocation
+ * would synchronise the device or is not allowed (inside a real-time frame
+ * callback, during another component's stream capture).  It allocates
+ * nothing: its scratch (per-pixel residuals, per-CTA partial sums, tickets
+ * and the solver state) is a fixed array of about 5.3 MB in the library's
+ * static device memory, present on every device that loads the library.
+ * Limits: width * height <= 640 * 480 and width, height >= 4; larger levels
+ * return YAS_ERR_CAPACITY.  mode: enum yas_track_mode.  dev_out (device,
+ * 46 doubles): H row-major (36), b (6), stats (4) as yas_tracker_compute_step.
+ * The first call on a device resolves the scratch address (no allocation);
+ * make that first call before capturing a stream.  All calls share the one
+ * scratch array, so calls whose GPU work overlaps (other streams, other host
+ * threads) race and must be serialised by the caller; the call itself only
+ * enqueues work on `stream` (NULL: legacy default stream). */
+YAS_API int yas_gn_linearise_static(const yas_gn_level *level, const yas_pose *T, int mode, double *dev_out,
+                                    void *stream);
+
 /* ---------------------------------------------------------------- session
  * One SLAM session: a submap, a raycaster and a tracker whose per-frame dense
  * work (Tracking::TrackRGBD + Tracking::StereoInitialization dense calls,

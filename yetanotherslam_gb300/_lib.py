@@ -51,6 +51,13 @@ class SessionConfig(C.Structure):
                 ("depth_scale", C.c_float), ("max_step_translation", C.c_float), ("use_graph", C.c_int)]
 
 
+class GnLevel(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
+                ("cy", C.c_float), ("ref_intensity", C.c_void_p), ("ref_inv_depth", C.c_void_p),
+                ("ref_vmap", C.c_void_p), ("ref_nmap", C.c_void_p), ("cur_intensity", C.c_void_p),
+                ("cur_gx", C.c_void_p), ("cur_gy", C.c_void_p), ("cur_vmap", C.c_void_p), ("cur_nmap", C.c_void_p)]
+
+
 _P = C.c_void_p
 _PP = C.POINTER(C.c_void_p)
 _I = C.c_int
@@ -125,6 +132,7 @@ _SIGS = {
     "yas_session_stream": [_P],
     "yas_session_profile_frame": [_P, _P, _P, _I, _P, _P, _I, _PI],
     "yas_mc_tables": [_P, _P, _P],
+    "yas_gn_linearise_static": [C.POINTER(GnLevel), C.POINTER(Pose), _I, _P, _P],
 }
 _RESTYPE = {"yas_status_string": C.c_char_p, "yas_version": C.c_char_p, "yas_session_stream": C.c_void_p}
 

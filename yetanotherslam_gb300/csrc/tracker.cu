@@ -808,3 +808,118 @@ void tracker_model(yas_tracker *tr, cudaStream_t s) {
 }
 
 }  // namespace yas
+
+// ---------------------------------------------------------------- linearisation without allocation
+// yas_gn_linearise_static runs the same kernels as yas_tracker_compute_step,
+// with every piece of scratch in one file-scope device array instead of
+// memory allocated by a tracker handle.
+namespace yas {
+
+constexpr int kStaticMaxPixels = 640 * 480;
+constexpr int kStaticMaxCtas = (kStaticMaxPixels + kTrackThreads - 1) / kTrackThreads;
+constexpr int kStaticGroups = (kStaticMaxCtas + (int)kGroup - 1) / (int)kGroup;
+
+struct StaticScratch {
+    GNState state;
+    float4 res4[kStaticMaxPixels];
+    float partialA[kStaticMaxCtas * 32];
+    float partialB[kStaticMaxCtas * 32];
+    float growA[kStaticGroups * 64];
+    float growB[kStaticGroups * 64];
+    unsigned counters[2 * (kStaticGroups + 1)];  // pass A tickets, then pass B tickets
+};
+
+static __device__ __align__(256) StaticScratch g_static_scratch;
+
+// Device address of g_static_scratch per device, resolved once per device.
+static std::mutex g_static_mutex;
+static StaticScratch *g_static_ptr[64];
+
+static int static_scratch(StaticScratch **out) {
+    int dev = 0;
+    YAS_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return YAS_ERR_STATE;
+    std::lock_guard<std::mutex> lk(g_static_mutex);
+    if (!g_static_ptr[dev]) {
+        void *p = nullptr;
+        YAS_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+        g_static_ptr[dev] = static_cast<StaticScratch *>(p);
+    }
+    *out = g_static_ptr[dev];
+    return YAS_OK;
+}
+
+__global__ void copy_linearisation(const GNState *st, double *out) {
+    const int i = threadIdx.x;
+    if (i < 36) out[i] = st->H[i];
+    if (i < 6) out[36 + i] = st->b[i];
+    if (i < 4) out[42 + i] = st->stats[i];
+}
+
+}  // namespace yas
+
+extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas_pose *T, int mode, double *dev_out,
+                                               void *stream) {
+    using namespace yas;
+    if (!lv || !T || !dev_out) return YAS_ERR_BAD_ARG;
+    if (mode != YAS_TRACK_RGB && mode != YAS_TRACK_ICP && mode != YAS_TRACK_RGBD) return YAS_ERR_BAD_ARG;
+    if (lv->width < 4 || lv->height < 4 || !(lv->fx > 0.0f) || !(lv->fy > 0.0f)) return YAS_ERR_BAD_ARG;
+    if ((long long)lv->width * lv->height > kStaticMaxPixels) return YAS_ERR_CAPACITY;
+    if ((mode & YAS_TRACK_RGB) && (!lv->ref_intensity || !lv->ref_inv_depth || !lv->cur_intensity || !lv->cur_gx ||
+                                   !lv->cur_gy))
+        return YAS_ERR_BAD_ARG;
+    if ((mode & YAS_TRACK_ICP) && (!lv->ref_vmap || !lv->ref_nmap || !lv->cur_vmap || !lv->cur_nmap))
+        return YAS_ERR_BAD_ARG;
+    StaticScratch *sc = nullptr;
+    YAS_TRY(static_scratch(&sc));
+    cudaStream_t s = (cudaStream_t)stream;
+    // tickets must start at zero; everything else is written before it is read
+    YAS_TRY_CUDA(cudaMemsetAsync(sc->counters, 0, sizeof(sc->counters), s));
+    PassArgs a;
+    memset(&a, 0, sizeof(a));
+    a.c.fx = lv->fx;
+    a.c.fy = lv->fy;
+    a.c.cx = lv->cx;
+    a.c.cy = lv->cy;
+    a.c.invfx = (float)(1.0 / (double)lv->fx);
+    a.c.invfy = (float)(1.0 / (double)lv->fy);
+    a.c.w = lv->width;
+    a.c.h = lv->height;
+    a.level = 0;
+    a.mode = mode;
+    a.first_of_level = 0;
+    a.no_update = 1;
+    a.L = 1;
+    a.angle_th = sinf(20.f * 3.14159254f / 180.f);
+    a.dist_th = 0.01f;
+    a.ref_int = lv->ref_intensity;
+    a.ref_invd = lv->ref_inv_depth;
+    a.ref_vmap = reinterpret_cast<const float4 *>(lv->ref_vmap);
+    a.ref_nmap = reinterpret_cast<const float4 *>(lv->ref_nmap);
+    a.cur_int = lv->cur_intensity;
+    a.cur_gx = lv->cur_gx;
+    a.cur_gy = lv->cur_gy;
+    a.cur_vmap = reinterpret_cast<const float4 *>(lv->cur_vmap);
+    a.cur_nmap = reinterpret_cast<const float4 *>(lv->cur_nmap);
+    a.res4 = sc->res4;
+    a.st = &sc->state;
+    a.Kd[0][0] = lv->fx;
+    a.Kd[0][1] = lv->fy;
+    a.Kd[0][2] = lv->cx;
+    a.Kd[0][3] = lv->cy;
+    gn_init_kernel<<<1, 32, 0, s>>>(a.st, pose_from(*T), 1, a);
+    const int g = pass_grid(a.c);
+    a.partial = sc->partialA;
+    a.grow = sc->growA;
+    a.counter = sc->counters;
+    gn_pass_a<<<g, kTrackThreads, 0, s>>>(a);
+    if (mode & YAS_TRACK_RGB) {
+        a.partial = sc->partialB;
+        a.grow = sc->growB;
+        a.counter = sc->counters + kStaticGroups + 1;
+        gn_pass_b<<<g, kTrackThreads, 0, s>>>(a);
+    }
+    copy_linearisation<<<1, 64, 0, s>>>(a.st, dev_out);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
