@@ -99,6 +99,9 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+GN_ITERS = (10, 5, 3)
+
+
 def make_frames(n: int, w: int, h: int, seed: int):
     from yetanotherslam_gb300 import synth
 
@@ -114,11 +117,14 @@ def stage_bytes(stage: int, P: list[int], nvis: int, vbytes: int, P0: int) -> fl
         return 20.0 * P[stage - 20]
     if stage == 9:  # integration: voxels read+write, depth map, keys + visible list
         return nvis * 512 * 2 * vbytes + 4.0 * P0 + nvis * 12.0
+    if stage == 30:  # fused GN schedule: per iteration and pixel, the pass-A reads
+        # (ref inverse depth + intensity 8, current intensity/gradients 12, four float4 maps 64)
+        return float(sum(84.0 * it * p for it, p in zip(GN_ITERS, P)))
     return float("nan")
 
 
 STAGE_NAMES = {0: "image_pyramid", 1: "depth_pyramid", 2: "zrange", 3: "ray_march", 4: "model_pyramid",
-               5: "gn_init", 6: "finalize", 7: "allocate", 8: "visibility", 9: "integrate"}
+               5: "gn_init", 6: "finalize", 7: "allocate", 8: "visibility", 9: "integrate", 30: "gauss_newton"}
 
 
 def stage_name(s: int) -> str:
@@ -155,7 +161,7 @@ def run_gpu(args):
     def new_session():
         return rf.Session(W, H, K, hash_slots=WORKLOAD["hash_slots"], max_blocks=WORKLOAD["max_blocks"],
                           voxel_size=WORKLOAD["voxel_m"], trunc_dist=WORKLOAD["trunc_m"],
-                          voxel_format=rf.VOXEL_F16, num_levels=3, iterations=(10, 5, 3), use_graph=True)
+                          voxel_format=rf.VOXEL_F16, num_levels=3, iterations=GN_ITERS, use_graph=True)
 
     # ---------------- device-resident inputs (value)
     dev_rgb = [torch.from_numpy(f.rgb).cuda() for f in frames[:nframes]]

@@ -44,7 +44,8 @@ enum yas_status {
     YAS_ERR_MESH_OVERFLOW = 8, /* more triangles than the mesher's capacity  */
     YAS_ERR_STATE = 9,         /* call not valid in the handle's state       */
     YAS_ERR_COORD_RANGE = 10,  /* block coordinate outside the 21-bit range  */
-    YAS_ERR_CAPACITY = 11      /* caller buffer too small                    */
+    YAS_ERR_CAPACITY = 11,     /* caller buffer too small                    */
+    YAS_ERR_TIMEOUT = 12       /* a bounded device-side wait gave up         */
 };
 
 /* Human-readable name of a status code (static string). */
@@ -208,6 +209,11 @@ YAS_API int yas_tracker_set_reference_model(yas_tracker *tr, const float *dev_vm
 /* GetTransform(init, bSwapBuffer): RGBDTracking.h:27 / RGBDTracking.cu:152-214. */
 YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int swap_buffer,
                                       yas_pose *out);
+/* No counterpart in the reference: 1 (default) runs GetTransform's whole
+ * coarse-to-fine schedule as one cooperative launch; 0 launches the two
+ * pixel passes of every iteration separately.  Results agree within the
+ * rounding of a different summation order. */
+YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused);
 /* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);
@@ -277,6 +283,7 @@ typedef struct yas_session_config {
     float depth_scale;     /* metres per depth unit (u16 mm: 0.001)          */
     float max_step_translation; /* frame-step rejection, reference 0.1 m     */
     int use_graph;         /* 1: capture the frame into a CUDA graph          */
+    int fused_schedule;    /* 1: all GN iterations in one cooperative launch  */
 } yas_session_config;
 
 YAS_API int yas_session_config_default(yas_session_config *cfg, int width, int height,

@@ -62,6 +62,21 @@ def test_graph_and_eager_are_identical(cuda):
     assert sa.kernels_per_frame() > 0
 
 
+def test_fused_and_per_iteration_schedules_agree(cuda):
+    W, H, n = 320, 240, 8
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, n, W, H)
+    sa = rf.Session(W, H, K, hash_slots=1 << 20, max_blocks=1 << 17, voxel_size=0.008, fused_schedule=True)
+    sb = rf.Session(W, H, K, hash_slots=1 << 20, max_blocks=1 << 17, voxel_size=0.008, fused_schedule=False)
+    for i, (rgb, d16, _, _) in enumerate(seq):
+        st_a, A = sa.process(rgb, d16)
+        st_b, B = sb.process(rgb, d16)
+        assert st_a == 0 and st_b == 0
+        dt, dr = pose_error(A, B)
+        assert dt <= 1e-5 and dr <= 1e-5, f"frame {i}: {dt:.3g} m {dr:.3g} rad"
+    assert sa.kernels_per_frame() < sb.kernels_per_frame()
+
+
 def test_device_resident_inputs(cuda):
     import torch
 

@@ -19,7 +19,7 @@ YAS_OK = 0
 STATUS = {
     0: "YAS_OK", 1: "YAS_ERR_BAD_ARG", 2: "YAS_ERR_OOM", 3: "YAS_ERR_CUDA", 4: "YAS_ERR_TABLE_FULL",
     5: "YAS_ERR_POOL_FULL", 6: "YAS_ERR_NUMERIC", 7: "YAS_ERR_TRACK_LOST", 8: "YAS_ERR_MESH_OVERFLOW",
-    9: "YAS_ERR_STATE", 10: "YAS_ERR_COORD_RANGE", 11: "YAS_ERR_CAPACITY",
+    9: "YAS_ERR_STATE", 10: "YAS_ERR_COORD_RANGE", 11: "YAS_ERR_CAPACITY", 12: "YAS_ERR_TIMEOUT",
 }
 VOXEL_F32, VOXEL_F16, VOXEL_S24 = 0, 1, 2
 TRACK_RGB, TRACK_ICP, TRACK_RGBD = 1, 2, 3
@@ -48,7 +48,8 @@ class MapConfig(C.Structure):
 class SessionConfig(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("K", Intrinsics), ("map", MapConfig),
                 ("num_levels", C.c_int), ("iterations", C.c_int * 5), ("mode", C.c_int),
-                ("depth_scale", C.c_float), ("max_step_translation", C.c_float), ("use_graph", C.c_int)]
+                ("depth_scale", C.c_float), ("max_step_translation", C.c_float), ("use_graph", C.c_int),
+                ("fused_schedule", C.c_int)]
 
 
 class GnLevel(C.Structure):
@@ -114,6 +115,7 @@ _SIGS = {
     "yas_tracker_get_transform": [_P, C.POINTER(Pose), _I, C.POINTER(Pose)],
     "yas_tracker_swap_frame_buffer": [_P],
     "yas_tracker_is_good": [_P, _PI],
+    "yas_tracker_set_schedule": [_P, _I],
     "yas_tracker_compute_step": [_P, _I, C.POINTER(Pose), _P, _P, _P],
     "yas_tracker_level_buffer": [_P, _I, _I, _PP, _PI, _PI, _PI],
     "yas_session_config_default": [C.POINTER(SessionConfig), _I, _I, C.POINTER(Intrinsics), _I, _I,

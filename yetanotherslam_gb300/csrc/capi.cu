@@ -150,6 +150,7 @@ YAS_API const char *yas_status_string(int s) {
         case YAS_ERR_STATE: return "invalid state for this call";
         case YAS_ERR_COORD_RANGE: return "block coordinate outside the key range";
         case YAS_ERR_CAPACITY: return "caller buffer too small";
+        case YAS_ERR_TIMEOUT: return "device-side wait timed out";
         default: return "unknown status";
     }
 }
@@ -827,7 +828,7 @@ YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int
     if (st.failed) {
         tr->good = false;
         *out = pose_to(pose_identity());
-        return YAS_ERR_NUMERIC;
+        return st.failed == kFailTimeout ? YAS_ERR_TIMEOUT : YAS_ERR_NUMERIC;
     }
     yas_pose r;
     for (int i = 0; i < 12; ++i) r.m[i] = st.best[i];
@@ -840,6 +841,12 @@ YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr) {
     if (!tr) return YAS_ERR_BAD_ARG;
     tr->cur = 1 - tr->cur;
+    return YAS_OK;
+}
+
+YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused) {
+    if (!tr) return YAS_ERR_BAD_ARG;
+    tr->use_fused = fused != 0;
     return YAS_OK;
 }
 

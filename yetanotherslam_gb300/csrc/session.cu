@@ -84,7 +84,7 @@ __global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float m
         const double tn2 = D[3] * D[3] + D[7] * D[7] + D[11] * D[11];
         ok = 1;
         if (st->failed) {
-            fs->status = YAS_ERR_NUMERIC;
+            fs->status = st->failed == kFailTimeout ? YAS_ERR_TIMEOUT : YAS_ERR_NUMERIC;
             fs->skip = 1;
             ok = 0;
         } else if (!(tn2 <= (double)max_t * (double)max_t)) {
@@ -259,6 +259,7 @@ YAS_API int yas_session_config_default(yas_session_config *cfg, int width, int h
     cfg->depth_scale = 0.001f;
     cfg->max_step_translation = 0.1f;
     cfg->use_graph = 1;
+    cfg->fused_schedule = 1;
     return YAS_OK;
 }
 
@@ -286,6 +287,7 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
         const double K[9] = {cfg->K.fx, 0, cfg->K.cx, 0, cfg->K.fy, cfg->K.cy, 0, 0, 1};
         st = yas_tracker_create(&s->tr, cfg->width, cfg->height, K, cfg->num_levels, cfg->iterations, cfg->mode,
                                 s->stream);
+        if (st == YAS_OK) st = yas_tracker_set_schedule(s->tr, cfg->fused_schedule);
     }
     if (st == YAS_OK) {
         const size_t n = (size_t)cfg->width * cfg->height;

@@ -31,9 +31,11 @@
 // host between iterations, so a whole frame can be captured in a CUDA graph.
 // Per-thread sums cover at most 4 pixels before the pairwise tree, so the FP32
 // part of every reduction is pairwise.
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 
+#include "gn_solve.cuh"
 #include "yas_track.h"
 
 namespace yas {
@@ -100,41 +102,49 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // (shared) holds the totals.  counters[0] is the grid ticket, counters[1+g]
 // the ticket of group g; each is reset by the CTA that consumes it.
 constexpr unsigned kGroup = 32;
+constexpr unsigned kSubsets = kTrackThreads / 32;  // reduction subsets (= warps)
 
-__device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float *grow, unsigned *counters,
-                                              double *tot) {
-    constexpr unsigned S = kTrackThreads / 32;  // subsets (= warps)
-    __shared__ float wsum[S][32];
-    __shared__ float lsum[S][32];
-    __shared__ double dsum[S][32];
-    __shared__ bool flag;
+// Stage 1: the CTA's FP32 row of 32 sums, stored to `row` (visible GPU-wide
+// before the function returns).
+__device__ __forceinline__ void cta_row32(float v[32], float *row) {
+    __shared__ float wsum[kSubsets][32];
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    const unsigned c = threadIdx.x & 31, sub = threadIdx.x >> 5;
     float r = warp_transpose_reduce(v);
     wsum[warp][lane] = r;
     __syncthreads();
     if (threadIdx.x < 32) {
         float s = 0.0f;
 #pragma unroll
-        for (unsigned w = 0; w < S; ++w) s += wsum[w][threadIdx.x];
-        partial[blockIdx.x * 32 + threadIdx.x] = s;
+        for (unsigned w = 0; w < kSubsets; ++w) s += wsum[w][threadIdx.x];
+        row[threadIdx.x] = s;
         __threadfence();
     }
     __syncthreads();
-    const unsigned g = blockIdx.x / kGroup;
+}
+
+// Stage 2: CTA `cta` of `nact` takes a ticket of its group of kGroup CTAs; the
+// last to arrive folds the group's rows (compensated FP32) into the (hi, lo)
+// row grow[g], resets the ticket and returns true.
+__device__ __forceinline__ bool group_fold(const float *rows, float *grow, unsigned *ticket, unsigned cta,
+                                           unsigned nact) {
+    constexpr unsigned S = kSubsets;
+    __shared__ float wsum[S][32];
+    __shared__ float lsum[S][32];
+    __shared__ bool flag;
+    const unsigned c = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    const unsigned g = cta / kGroup;
     const unsigned g0 = g * kGroup;
-    const unsigned gsize = min(kGroup, gridDim.x - g0);
-    const unsigned ngroups = (gridDim.x + kGroup - 1) / kGroup;
-    if (threadIdx.x == 0) flag = (atomicAdd(&counters[1 + g], 1u) == gsize - 1);
+    const unsigned gsize = min(kGroup, nact - g0);
+    if (threadIdx.x == 0) flag = (atomicAdd(&ticket[g], 1u) == gsize - 1);
     __syncthreads();
     if (!flag) return false;
     __threadfence();
-    {  // group level: subset `sub` folds rows g0 + sub + S*q
+    {  // subset `sub` folds rows g0 + sub + S*q
         float h = 0.0f, l = 0.0f, x[kGroup / S];
 #pragma unroll
         for (unsigned q = 0; q < kGroup / S; ++q) {
             const unsigned row = sub + S * q;
-            x[q] = row < gsize ? __ldcg(partial + (g0 + row) * 32 + c) : 0.0f;
+            x[q] = row < gsize ? __ldcg(rows + (g0 + row) * 32 + c) : 0.0f;
         }
 #pragma unroll
         for (unsigned q = 0; q < kGroup / S; ++q) {
@@ -158,15 +168,26 @@ __device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float
         }
         grow[g * 64 + c] = h;
         grow[g * 64 + 32 + c] = l;
-        __threadfence();
     }
-    if (threadIdx.x == 0) counters[1 + g] = 0u;
+    if (threadIdx.x == 0) atomicExch(&ticket[g], 0u);
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) flag = (atomicAdd(&counters[0], 1u) == ngroups - 1);
+    return true;
+}
+
+// Stage 3: a group folder takes the grid ticket; the last of the `ngroups`
+// folds the group rows (compensated FP32 per subset, subsets added in FP64)
+// into tot[0..31] (shared), resets the ticket and returns true.
+__device__ __forceinline__ bool grid_fold(const float *grow, unsigned *ticket, unsigned ngroups, double *tot) {
+    constexpr unsigned S = kSubsets;
+    __shared__ double dsum[S][32];
+    __shared__ bool flag;
+    const unsigned c = threadIdx.x & 31, sub = threadIdx.x >> 5;
+    if (threadIdx.x == 0) flag = (atomicAdd(ticket, 1u) == ngroups - 1);
     __syncthreads();
     if (!flag) return false;
     __threadfence();
-    {  // grid level: subset `sub` folds group rows sub, sub + S, ...
+    {
         float h = 0.0f, l = 0.0f;
         for (unsigned row = sub; row < ngroups; row += 2 * S) {
             const float xh0 = __ldcg(grow + row * 64 + c), xl0 = __ldcg(grow + row * 64 + 32 + c);
@@ -190,16 +211,19 @@ __device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float
         for (unsigned k = 0; k < S; ++k) s += dsum[k][threadIdx.x];
         tot[threadIdx.x] = s;
     }
-    if (threadIdx.x == 0) counters[0] = 0u;
+    if (threadIdx.x == 0) atomicExch(ticket, 0u);
     __syncthreads();
     return true;
 }
 
-// ---------------------------------------------------------------- FP64 algebra
-// FP64 on GB300 has a dependent latency of about 65 cycles (16x FP32) and an
-// IEEE FP64 division is a multi-step sequence; the solve therefore avoids
-// divisions (FP32-seeded reciprocals, polynomial series for small angles).
+__device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float *grow, unsigned *counters,
+                                              double *tot) {
+    cta_row32(v, partial + blockIdx.x * 32);
+    if (!group_fold(partial, grow, counters + 1, blockIdx.x, gridDim.x)) return false;
+    return grid_fold(grow, counters, (gridDim.x + kGroup - 1) / kGroup, tot);
+}
 
+// ---------------------------------------------------------------- estimate helpers
 // Float copy of the estimate read by the pixel passes.
 __device__ void publish_estimate(GNState *st, const double Kd[kMaxLevels][4], int L) {
     (void)Kd;
@@ -220,256 +244,6 @@ __device__ __forceinline__ void make_rkinv(const float *T, const LevelCam &c, fl
     }
 }
 
-// Packed index k of the 28 products of [J | r]: rows i, columns j >= i
-// (RankUpdateHessian<6,7>, TrackingUtils.h:45-58).
-__constant__ signed char c_pack_i[27] = {0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 5, 5};
-// Taylor coefficients (in th^2) of sin(th)/th, (1-cos th)/th^2, (th-sin th)/th^3.
-__constant__ double c_exp_poly[3][5] = {
-    {1.0, -1.0 / 6.0, 1.0 / 120.0, -1.0 / 5040.0, 1.0 / 362880.0},
-    {0.5, -1.0 / 24.0, 1.0 / 720.0, -1.0 / 40320.0, 1.0 / 3628800.0},
-    {1.0 / 6.0, -1.0 / 120.0, 1.0 / 5040.0, -1.0 / 362880.0, 1.0 / 39916800.0}};
-__constant__ signed char c_pack_j[27] = {0, 1, 2, 3, 4, 5, 6, 1, 2, 3, 4, 5, 6, 2, 3, 4, 5, 6, 3, 4, 5, 6, 4, 5, 6, 5, 6};
-
-// Reciprocal for the solve: FP32 seed and one Newton step in FP64 (relative
-// error below 2^-46, far under the ~1e-7 precision of the FP32-accumulated
-// system it is applied to).
-__device__ __forceinline__ double drcp1(double d) {
-    const double ad = fabs(d);
-    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
-    const double r = (double)__frcp_rn((float)d);
-    return fma(r, fma(-d, r, 1.0), r);
-}
-
-__device__ __forceinline__ int pack_index(int r, int c) { return 7 * r - (r * (r - 1)) / 2 + c - r; }
-
-// The solve of one Gauss-Newton iteration, executed by the 32 lanes of warp 0
-// of the final CTA (GetTransform's loop body, RGBDTracking.cu:184-207):
-//   H = H_rgb + 100 H_icp, b = b_rgb + 10 b_icp (RGBDTracking.cu:543-544);
-//   error = sqrt(residualSum) / (numResidual + 6), in FP32 as the reference;
-//   update = LDLT(H).solve(b) in FP64: LDL^T with diagonal pivoting (largest
-//   remaining diagonal, first on ties, left-looking), pseudo-inverse of D
-//   (|d| <= 1/DBL_MAX -> 0), identity transpositions and no factorisation if
-//   the first pivot is zero (Eigen 3's LDLT);
-//   NaN in update(0): the iteration fails and the result is the identity;
-//   estimate = exp(update) * estimate (SE(3) exponential, FP64);
-//   the kept estimate is the one after an update whose error beat the level's.
-// GB300's dependent FP64 latency is ~65 cycles, so the solve keeps row i of H
-// in the registers of lane i, moves columns between lanes with shuffles, runs
-// every independent FP64 product on its own lane, and unrolls the
-// factorisation so that every register index is static.
-__device__ __noinline__ void gn_solve_warp(const PassArgs &a) {
-    __shared__ double Ls[36];
-    GNState *st = a.st;
-    const int lane = (int)(threadIdx.x & 31);
-    const double *A = st->a_sums, *B = st->b_sums;
-    const bool rowlane = lane < 6;
-    // ---- assemble row `lane` of H and b[lane]
-    double row[6], y = 0.0;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        row[j] = 0.0;
-        if (rowlane) {
-            const int kk = pack_index(min(lane, j), max(lane, j));
-            row[j] = a.mode == YAS_TRACK_RGBD ? fma(100.0, A[kk], B[kk]) : (a.mode == YAS_TRACK_RGB ? B[kk] : A[kk]);
-        }
-    }
-    if (rowlane) {
-        const int kk = pack_index(lane, 6);
-        y = a.mode == YAS_TRACK_RGBD ? fma(10.0, A[kk], B[kk]) : (a.mode == YAS_TRACK_RGB ? B[kk] : A[kk]);
-#pragma unroll
-        for (int j = 0; j < 6; ++j) st->H[lane * 6 + j] = row[j];
-        st->b[lane] = y;
-    }
-    const double residualSum = (double)(float)(a.mode == YAS_TRACK_RGB ? B[27] : A[27]);
-    const double numResidual = (double)(float)(a.mode == YAS_TRACK_ICP ? A[28] : A[29]);
-    if (lane == 0) {
-        st->stats[0] = residualSum;
-        st->stats[1] = numResidual;
-        st->stats[2] = st->huber_th;
-        st->stats[3] = A[28];
-    }
-    if (a.no_update) return;
-    const float error = sqrtf((float)residualSum) / ((float)numResidual + 6.0f);
-    // ---- LDL^T with diagonal pivoting
-    double Dv[6];
-    int trk[6];
-    bool broke = false;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        Dv[k] = 0.0;
-        trk[k] = k;
-        if (broke) continue;
-        // pivot: largest |diagonal| over rows k..5, first one on ties; a NaN
-        // never wins (every comparison with it is false) and a NaN at row k
-        // keeps row k; non-negative doubles order like their bit patterns
-        double diag = 0.0;
-#pragma unroll
-        for (int q = 0; q < 6; ++q)
-            if (lane == q) diag = row[q];
-        long long key = (lane >= k && lane < 6) ? (isnan(diag) ? -1LL : __double_as_longlong(fabs(diag))) : -2LL;
-        const long long keyk = __shfl_sync(0xffffffffu, key, k);
-        int p = k;
-        if (keyk >= 0) {
-            long long bk = key;
-            int bl = lane;
-#pragma unroll
-            for (int off = 1; off < 8; off <<= 1) {
-                const long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
-                const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
-                if (ok > bk || (ok == bk && ol < bl)) {
-                    bk = ok;
-                    bl = ol;
-                }
-            }
-            p = __shfl_sync(0xffffffffu, bl, 0);
-        }
-        trk[k] = p;
-        if (p != k) {
-            // rows k and p change lanes, then every row swaps columns k and p
-            const int src = lane == k ? p : (lane == p ? k : lane);
-#pragma unroll
-            for (int q = 0; q < 6; ++q) row[q] = __shfl_sync(0xffffffffu, row[q], src);
-#pragma unroll
-            for (int q = k + 1; q < 6; ++q)
-                if (q == p) {
-                    const double t = row[k];
-                    row[k] = row[q];
-                    row[q] = t;
-                }
-        }
-        if (k > 0) {
-            double tmp[6];
-#pragma unroll
-            for (int j = 0; j < k; ++j) tmp[j] = Dv[j] * __shfl_sync(0xffffffffu, row[j], k);
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < k; ++j) s = fma(row[j], tmp[j], s);
-            if (lane >= k) row[k] -= s;
-        }
-        const double d = __shfl_sync(0xffffffffu, row[k], k);
-        Dv[k] = d;
-        const bool valid = fabs(d) > 0.0;
-        if (k == 0 && !valid) {
-            broke = true;  // identity transpositions, the matrix is used as it is
-            continue;
-        }
-        if (valid && lane > k) row[k] *= drcp1(d);
-    }
-    // ---- y = P b; L y' = y; D y'' = y'; L^T x = y''; x = P^T x
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const int p = trk[k];
-        const int src = lane == k ? p : (lane == p ? k : lane);
-        y = __shfl_sync(0xffffffffu, y, src);
-    }
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        const double yj = __shfl_sync(0xffffffffu, y, j);
-        if (lane > j && rowlane) y = fma(-row[j], yj, y);
-    }
-    {
-        double dd = 0.0;
-#pragma unroll
-        for (int q = 0; q < 6; ++q)
-            if (lane == q) dd = row[q];
-        y = (rowlane && fabs(dd) > 1.0 / DBL_MAX) ? y * drcp1(dd) : 0.0;
-    }
-    if (rowlane) {
-#pragma unroll
-        for (int q = 0; q < 6; ++q) Ls[lane * 6 + q] = row[q];
-    }
-    __syncwarp();
-#pragma unroll
-    for (int j = 5; j > 0; --j) {
-        const double yj = __shfl_sync(0xffffffffu, y, j);
-        const double lji = rowlane ? Ls[j * 6 + lane] : 0.0;  // L(j, lane)
-        if (lane < j) y = fma(-lji, yj, y);
-    }
-#pragma unroll
-    for (int k = 5; k >= 0; --k) {
-        const int p = trk[k];
-        const int src = lane == k ? p : (lane == p ? k : lane);
-        y = __shfl_sync(0xffffffffu, y, src);
-    }
-    double u[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) u[q] = __shfl_sync(0xffffffffu, y, q);
-    if (lane < 6) st->last_update[lane] = y;
-    if (isnan(u[0])) {
-        if (lane == 0) st->failed = 1;
-        if (lane < 12) st->best[lane] = (lane % 5 == 0) ? 1.0 : 0.0;
-        return;
-    }
-    // ---- SE(3) exponential, one matrix entry per lane:
-    // R = I + A W + B W^2, t = V v, V = I + B W + C W^2, W = hat(w),
-    // W^2 = w w^T - th^2 I, W v = w x v
-    const double wx = u[3], wy = u[4], wz = u[5];
-    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
-    double cA, cB, cC;
-    if (th2 < 1e-2) {
-        // Taylor series in th^2 to the th^8 term (truncation below 3e-18)
-        cA = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[0][4], c_exp_poly[0][3]), c_exp_poly[0][2]), c_exp_poly[0][1]),
-                 c_exp_poly[0][0]);
-        cB = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[1][4], c_exp_poly[1][3]), c_exp_poly[1][2]), c_exp_poly[1][1]),
-                 c_exp_poly[1][0]);
-        cC = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[2][4], c_exp_poly[2][3]), c_exp_poly[2][2]), c_exp_poly[2][1]),
-                 c_exp_poly[2][0]);
-    } else {
-        const double th = sqrt(th2);
-        double sn, cs;
-        sincos(th, &sn, &cs);
-        cA = sn / th;
-        cB = (1.0 - cs) / th2;
-        cC = (th - sn) / (th2 * th);
-    }
-    const double w[3] = {wx, wy, wz};
-    const int i = (lane < 12) ? lane / 4 : 0, jc = (lane < 12) ? lane % 4 : 0;
-    // row i of E: E(i,q) = d(i,q) + A W(i,q) + B (w_i w_q - d(i,q) th^2)
-    double Er[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const double Wiq = (i == q) ? 0.0
-                                    : ((i == 0 && q == 1) ? -wz
-                                       : (i == 0 && q == 2) ? wy
-                                       : (i == 1 && q == 0) ? wz
-                                       : (i == 1 && q == 2) ? -wx
-                                       : (i == 2 && q == 0) ? -wy
-                                                            : wx);
-        const double dq = (i == q) ? 1.0 : 0.0;
-        Er[q] = fma(cA, Wiq, fma(cB, fma(w[i], w[q], -dq * th2), dq));
-    }
-    // t_i = v_i + B (w x v)_i + C (w_i (w . v) - th^2 v_i)
-    const double wxv[3] = {wy * u[2] - wz * u[1], wz * u[0] - wx * u[2], wx * u[1] - wy * u[0]};
-    const double wdv = fma(wx, u[0], fma(wy, u[1], wz * u[2]));
-    const double ti = fma(cB, wxv[i], fma(cC, fma(w[i], wdv, -th2 * u[i]), u[i]));
-    // ---- estimate = E * estimate, entry (i, jc) on lane i*4 + jc
-    double o = 0.0;
-    if (lane < 12) {
-        const double e0 = st->est[0 * 4 + jc], e1 = st->est[1 * 4 + jc], e2 = st->est[2 * 4 + jc];
-        o = fma(Er[0], e0, fma(Er[1], e1, Er[2] * e2));
-        if (jc == 3) o += ti;
-    }
-    __syncwarp();
-    if (lane < 12) {
-        st->est[lane] = o;
-        st->Tf[lane] = (float)o;
-    }
-    // ---- acceptance on the error measured before the update
-    int accept = 0;
-    if (lane == 0) {
-        if (a.first_of_level) st->last_error = (double)FLT_MAX;
-        accept = (double)error < st->last_error;
-        if (accept) {
-            st->last_error = (double)error;
-            st->n_success++;
-        }
-        st->n_iter++;
-        st->level_of_last = a.level;
-    }
-    accept = __shfl_sync(0xffffffffu, accept, 0);
-    if (accept && lane < 12) st->best[lane] = o;
-}
-
 // ---------------------------------------------------------------- pixel math
 // TransformReferencePoint (ImageProc.cu:42-78): (RKinv (x,y,1)) z + t, fixed order.
 __device__ __forceinline__ float3 warp_ref_point(const float *RK, const float *T, int x, int y, float z) {
@@ -487,6 +261,20 @@ __device__ __forceinline__ float bilinear(const float *__restrict__ m, int w, fl
     const float *r0 = m + (size_t)v * w + u, *r1 = r0 + w;
     return (__ldg(r0) * (1.0f - cx) + __ldg(r0 + 1) * cx) * (1.0f - cy) +
            (__ldg(r1) * (1.0f - cx) + __ldg(r1 + 1) * cx) * cy;
+}
+
+// Huber threshold 4.685 * stddev of the photometric residuals, in FP32 as the
+// reference (RGBDTracking.cu:259-278), from the FP64 totals n = tot[29],
+// sum r = tot[30], sum r^2 = tot[31]: mean = sum r / n, then
+// sum (r - mean)^2 = sum r^2 - 2 mean sum r + n mean^2 (the reference's second
+// pass over the residuals).
+__device__ __forceinline__ float huber_threshold(const double *tot) {
+    const double nn = tot[29], s = tot[30], s2 = tot[31];
+    const float mean = (float)s / (float)nn;
+    const double md = (double)mean;
+    const double ss = fma(nn * md, md, fma(-2.0 * md, s, s2));
+    const float var = sqrtf((float)ss / ((float)nn - 1.0f));
+    return (float)(4.685 * (double)var);
 }
 
 __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
@@ -574,22 +362,16 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
     }
     if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
     if (threadIdx.x < 32) st->a_sums[threadIdx.x] = tot[threadIdx.x];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        // Huber threshold 4.685 * stddev of the photometric residuals, in FP32
-        // as the reference (RGBDTracking.cu:259-278): mean = sum r / n, then
-        // sum (r - mean)^2 = sum r^2 - 2 mean sum r + n mean^2 from the FP64
-        // totals (the reference's second pass over the residuals).
-        const double nn = tot[29], s = tot[30], s2 = tot[31];
-        const float mean = (float)s / (float)nn;
-        const double md = (double)mean;
-        const double ss = fma(nn * md, md, fma(-2.0 * md, s, s2));
-        const float var = sqrtf((float)ss / ((float)nn - 1.0f));
-        st->huber_th = (float)(4.685 * (double)var);
-    }
+    if (threadIdx.x == 0) st->huber_th = huber_threshold(tot);
     if (a.mode == YAS_TRACK_ICP) {
+        load_solve_state(st);
+        if (threadIdx.x < 32) g_solve.A[threadIdx.x] = tot[threadIdx.x];
+        if (threadIdx.x == 0) g_solve.huber_th = huber_threshold(tot);
         __syncthreads();
-        if (threadIdx.x < 32) gn_solve_warp(a);
+        if (threadIdx.x < 32) {
+            gn_solve(a.mode, a.no_update, a.first_of_level, a.level);
+            publish_solve(st);
+        }
     }
 }
 
@@ -633,9 +415,18 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_b(PassArgs a) {
         }
     }
     if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
-    if (threadIdx.x < 32) st->b_sums[threadIdx.x] = tot[threadIdx.x];
+    load_solve_state(st);
+    if (threadIdx.x < 32) {
+        st->b_sums[threadIdx.x] = tot[threadIdx.x];
+        g_solve.B[threadIdx.x] = tot[threadIdx.x];
+        g_solve.A[threadIdx.x] = __ldcg(&st->a_sums[threadIdx.x]);
+    }
+    if (threadIdx.x == 0) g_solve.huber_th = th;
     __syncthreads();
-    if (threadIdx.x < 32) gn_solve_warp(a);
+    if (threadIdx.x < 32) {
+        gn_solve(a.mode, a.no_update, a.first_of_level, a.level);
+        publish_solve(st);
+    }
 }
 
 __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) {
@@ -650,7 +441,408 @@ __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) 
     st->n_iter = 0;
     st->n_success = 0;
     st->level_of_last = -1;
+    st->huber_th = 0.0f;
+    st->epoch += 1u;  // tags of the fused schedule's rows differ from every earlier launch
+    st->abort_word = 0u;
     publish_estimate(st, kargs.Kd, L);
+}
+
+// ---------------------------------------------------------------- fused schedule
+// One cooperative launch runs every Gauss-Newton iteration of every level
+// (GetTransform's loops, RGBDTracking.cu:161-208), one 1024-thread CTA per SM,
+// CTA c owning the pixel range [c * chunk, (c + 1) * chunk) of each level.
+// Nothing is released by one CTA to the others: each CTA publishes its row
+// of partial sums as tagged 64-bit words {value, tag} (tag = launch epoch and
+// iteration), every CTA polls all rows until the tags match, folds them in
+// the same fixed order and runs the same solve, so every CTA holds the same
+// estimate without a barrier, a fence or an atomic:
+//   1. pass A (warp, photometric residual, ICP products) -> row A;
+//      [RGB] fold of the three photometric moments -> Huber threshold;
+//   2. [RGB] pass B (weighted photometric products, from the residuals each
+//      thread kept in registers) -> row B;
+//   3. fold of the ICP and photometric systems -> FP64 solve -> estimate.
+// Rows are double-buffered by iteration parity: a CTA can run at most one
+// iteration ahead of the slowest reader of a buffer.  Every wait is bounded by
+// a wall-clock limit: a CTA that gives up raises the state's abort word, every
+// waiter leaves as soon as it sees it, and the state reports kFailTimeout.
+// CTA 0 writes the final state to global memory.
+constexpr int kFusedThreads = 1024;
+constexpr int kFusedWarps = kFusedThreads / 32;
+constexpr int kFoldSubsets = 16;    // row subsets of the system fold
+constexpr int kFoldRows = 10;       // rows per subset
+constexpr int kFusedMaxCtas = kFoldSubsets * kFoldRows;  // 160
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+
+struct FusedLevel {
+    LevelCam c;
+    int iters;
+    int chunk;  // pixels per CTA (a multiple of 32)
+    int pix;    // pixels per thread, ceil(chunk / kFusedThreads)
+    const float *ref_int, *ref_invd;
+    const float4 *ref_vmap, *ref_nmap;
+    const float *cur_int, *cur_gx, *cur_gy;
+    const float4 *cur_vmap, *cur_nmap;
+};
+
+struct FusedArgs {
+    FusedLevel lv[kMaxLevels];
+    int L, mode;
+    float angle_th, dist_th;
+    unsigned long long *rows;  // [2 parities][2 passes][kFusedMaxCtas][32] tagged words
+    GNState *st;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long tagged(float x, unsigned tag) {
+    return ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(x);
+}
+
+__device__ __forceinline__ bool tag_is(unsigned long long w, unsigned tag) { return (unsigned)(w >> 32) == tag; }
+
+// One step of a bounded poll: false once the launch was aborted or this
+// thread's wait (started at t0) exceeded kWaitLimitNs, which it then reports.
+__device__ __forceinline__ bool poll_continue(GNState *st, unsigned spin, unsigned long long &t0) {
+    __nanosleep(spin < 32 ? 32 : 256);
+    if ((spin & 15u) != 15u) return true;
+    if (ld_relaxed_u32(&st->abort_word) != 0u) return false;
+    const unsigned long long now = global_ns();
+    if (t0 == 0ull) {
+        t0 = now;
+    } else if (now - t0 > kWaitLimitNs) {
+        st->failed = kFailTimeout;
+        atomicExch(&st->abort_word, 1u);
+        return false;
+    }
+    return true;
+}
+
+// Pass A for one pixel: the photometric residual (kept in registers for pass
+// B) and the ICP products, accumulated as gn_pass_a does.
+__device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float *sT, const float *sRK, int k,
+                                              bool do_rgb, bool do_icp, float angle_th, float dist_th,
+                                              float acc[32], float4 &res, float3 &p) {
+    const LevelCam &c = lv.c;
+    const int y = k / c.w, x = k - y * c.w;
+    res = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    p = make_float3(0.0f, 0.0f, 1.0f);
+    if (do_rgb) {
+        const float zinv = __ldg(lv.ref_invd + k);
+        if (zinv > 0.0f) {
+            const float z = 1.0f / zinv;
+            p = warp_ref_point(sRK, sT, x, y, z);
+            const float u = c.fx * p.x / p.z + c.cx;
+            const float v = c.fy * p.y / p.z + c.cy;
+            if (u > 0.0f && v > 0.0f && u < (float)(c.w - 1) && v < (float)(c.h - 1)) {
+                const float r = bilinear(lv.cur_int, c.w, u, v) - __ldg(lv.ref_int + k);
+                const float gx = bilinear(lv.cur_gx, c.w, u, v);
+                const float gy = bilinear(lv.cur_gy, c.w, u, v);
+                const bool ok = (gx * gx + gy * gy) > 0.0f && isfinite(r);
+                res = make_float4(r, gx, gy, ok ? 1.0f : -1.0f);
+                if (ok) {
+                    acc[29] += 1.0f;
+                    acc[30] += r;
+                    acc[31] += r * r;
+                }
+            }
+        }
+    }
+    if (do_icp) {
+        const float4 vm = __ldg(lv.ref_vmap + k);
+        if (vm.w >= 0.0f) {
+            const float3 vl = make_float3(sT[0] * vm.x + sT[1] * vm.y + sT[2] * vm.z + sT[3],
+                                          sT[4] * vm.x + sT[5] * vm.y + sT[6] * vm.z + sT[7],
+                                          sT[8] * vm.x + sT[9] * vm.y + sT[10] * vm.z + sT[11]);
+            const float invz = 1.0f / vl.z;
+            const int u = (int)floorf(c.fx * vl.x * invz + c.cx + 0.5f);
+            const int v = (int)floorf(c.fy * vl.y * invz + c.cy + 0.5f);
+            if (u >= 0 && v >= 0 && u < c.w && v < c.h) {
+                const float4 vc = __ldg(lv.cur_vmap + v * c.w + u);
+                if (vc.w >= 0.0f) {
+                    const float4 nm = __ldg(lv.ref_nmap + k);
+                    const float3 nl = make_float3(sT[0] * nm.x + sT[1] * nm.y + sT[2] * nm.z,
+                                                  sT[4] * nm.x + sT[5] * nm.y + sT[6] * nm.z,
+                                                  sT[8] * nm.x + sT[9] * nm.y + sT[10] * nm.z);
+                    const float4 nc = __ldg(lv.cur_nmap + v * c.w + u);
+                    const float dx = vl.x - vc.x, dy = vl.y - vc.y, dz = vl.z - vc.z;
+                    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float cx_ = nc.y * nl.z - nc.z * nl.y, cy_ = nc.z * nl.x - nc.x * nl.z,
+                                cz_ = nc.x * nl.y - nc.y * nl.x;
+                    const float angle = sqrtf(cx_ * cx_ + cy_ * cy_ + cz_ * cz_);
+                    if (angle < angle_th && dist <= dist_th && nm.w > 0.0f && nc.w > 0.0f) {
+                        float row[7];
+                        row[0] = nl.x;
+                        row[1] = nl.y;
+                        row[2] = nl.z;
+                        row[3] = vl.y * nl.z - vl.z * nl.y;
+                        row[4] = vl.z * nl.x - vl.x * nl.z;
+                        row[5] = vl.x * nl.y - vl.y * nl.x;
+                        row[6] = nl.x * (vc.x - vl.x) + nl.y * (vc.y - vl.y) + nl.z * (vc.z - vl.z);
+                        int q = 0;
+#pragma unroll
+                        for (int i = 0; i < 7; ++i)
+#pragma unroll
+                            for (int j = i; j < 7; ++j) acc[q++] += row[i] * row[j];
+                        acc[28] += 1.0f;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Pass B for one pixel kept from pass A (gn_pass_b's products).
+__device__ __forceinline__ void fused_pixel_b(const LevelCam &c, float th, const float4 &res, const float3 &p,
+                                              float acc[32]) {
+    const float zInv = 1.0f / p.z;
+    float wt = 1.0f;
+    if (fabsf(res.x) > th) wt = th / fabsf(res.x);
+    float row[7];
+    row[0] = res.y * c.fx * zInv;
+    row[1] = res.z * c.fy * zInv;
+    row[2] = -(row[0] * p.x + row[1] * p.y) * zInv;
+    row[3] = row[2] * p.y - res.z * c.fy;
+    row[4] = -row[2] * p.x + res.y * c.fx;
+    row[5] = -row[0] * p.y + row[1] * p.x;
+    row[6] = -res.x;
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+#pragma unroll
+        for (int j = i; j < 7; ++j) acc[q++] += wt * row[i] * row[j];
+}
+
+
+// The CTA's row of 32 sums (warp transpose sums, then a pairwise tree over
+// the 32 warp sums of each value), published by warp 0 as tagged words.
+__device__ __forceinline__ void fused_publish_row(float v[32], unsigned long long *row, unsigned tag) {
+    __shared__ float wsum[kFusedWarps][33];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const float r = warp_transpose_reduce(v);
+    wsum[warp][lane] = r;
+    __syncthreads();
+    if (warp == 0) {
+        float x[kFusedWarps];
+#pragma unroll
+        for (int w = 0; w < kFusedWarps; ++w) x[w] = wsum[w][lane];
+#pragma unroll
+        for (int s = kFusedWarps / 2; s >= 1; s >>= 1)
+#pragma unroll
+            for (int i = 0; i < s; ++i) x[i] += x[i + s];
+        st_relaxed_u64(row + lane, tagged(x[0], tag));
+    }
+}
+
+// Totals over all CTAs of the photometric moments (columns 29..31 of rows A)
+// into g_solve.A[29..31]; compensated FP32 per column (32 lanes x 5 rows,
+// then a butterfly), FP64 at the end.  False on abort or timeout.
+__device__ __forceinline__ bool fold_moments(const unsigned long long *rows, unsigned nrows, unsigned tag,
+                                             GNState *st) {
+    __shared__ float m3[3][kFusedMaxCtas];
+    const int t = (int)threadIdx.x;
+    bool mine = true;
+    if (t < 3 * (int)nrows) {
+        const int q = t / (int)nrows, r = t - q * (int)nrows;
+        const unsigned long long *p = rows + r * 32 + 29 + q;
+        unsigned long long w = ld_relaxed_u64(p);
+        unsigned long long t0 = 0ull;
+        for (unsigned spin = 0; !tag_is(w, tag); ++spin) {
+            if (!poll_continue(st, spin, t0)) {
+                mine = false;
+                break;
+            }
+            w = ld_relaxed_u64(p);
+        }
+        m3[q][r] = __uint_as_float((unsigned)w);
+    }
+    if (!__syncthreads_and(mine)) return false;
+    const int warp = t >> 5, lane = t & 31;
+    if (warp < 3) {
+        float h = 0.0f, l = 0.0f;
+#pragma unroll
+        for (int m = 0; m < (kFusedMaxCtas + 31) / 32; ++m) {
+            const int r = lane + 32 * m;
+            float s, e;
+            two_sum(h, r < (int)nrows ? m3[warp][r] : 0.0f, s, e);
+            h = s;
+            l += e;
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, h, off), ol = __shfl_xor_sync(0xffffffffu, l, off);
+            float s, e;
+            two_sum(h, oh, s, e);
+            h = s;
+            l = (l + ol) + e;
+        }
+        if (lane == 0) g_solve.A[29 + warp] = (double)h + (double)l;
+    }
+    __syncthreads();
+    return true;
+}
+
+// Totals over all CTAs of the ICP system (columns 0..28 of rows A) into
+// g_solve.A[0..28] and of the photometric system (columns 0..27 of rows B)
+// into g_solve.B[0..27] (zero for a term the mode does not use).  Thread t
+// folds column t % 64 over the rows of subset t / 64 (compensated FP32), then
+// a butterfly over the 16 subsets of each column; FP64 at the end.  False on
+// abort or timeout.
+__device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, const unsigned long long *rowsB,
+                                             unsigned nrows, unsigned tag, bool icp, bool rgb, GNState *st) {
+    __shared__ float hs[kFoldSubsets][65], ls[kFoldSubsets][65];
+    const int t = (int)threadIdx.x, c = t & 63, sub = t >> 6;
+    const bool need = (c < 29 && icp) || (c >= 32 && c < 60 && rgb);
+    bool mine = true;
+    float h = 0.0f, l = 0.0f;
+    if (need) {
+        const unsigned long long *base = c < 32 ? rowsA + c : rowsB + (c - 32);
+        unsigned long long w[kFoldRows];
+#pragma unroll
+        for (int q = 0; q < kFoldRows; ++q) {
+            const unsigned r = (unsigned)(sub + kFoldSubsets * q);
+            w[q] = r < nrows ? ld_relaxed_u64(base + r * 32) : tagged(0.0f, tag);
+        }
+        unsigned long long t0 = 0ull;
+        for (unsigned spin = 0;; ++spin) {
+            unsigned pend = 0u;
+#pragma unroll
+            for (int q = 0; q < kFoldRows; ++q)
+                if (!tag_is(w[q], tag)) pend |= 1u << q;
+            if (pend == 0u) break;
+            if (!poll_continue(st, spin, t0)) {
+                mine = false;
+                break;
+            }
+#pragma unroll
+            for (int q = 0; q < kFoldRows; ++q)
+                if ((pend >> q) & 1u) w[q] = ld_relaxed_u64(base + (sub + kFoldSubsets * q) * 32);
+        }
+#pragma unroll
+        for (int q = 0; q < kFoldRows; ++q) {
+            float s, e;
+            two_sum(h, __uint_as_float((unsigned)w[q]), s, e);
+            h = s;
+            l += e;
+        }
+    }
+    hs[sub][c] = h;
+    ls[sub][c] = l;
+    if (!__syncthreads_and(mine)) return false;
+    {  // warp w folds columns 2w and 2w + 1, lanes 0..15 / 16..31 = subsets
+        const int warp = t >> 5, lane = t & 31;
+        const int col = 2 * warp + (lane >> 4), s_ = lane & 15;
+        float h2 = hs[s_][col], l2 = ls[s_][col];
+#pragma unroll
+        for (int off = 8; off >= 1; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, h2, off), ol = __shfl_xor_sync(0xffffffffu, l2, off);
+            float s, e;
+            two_sum(h2, oh, s, e);
+            h2 = s;
+            l2 = (l2 + ol) + e;
+        }
+        if (s_ == 0) {
+            const double v = (double)h2 + (double)l2;
+            if (col < 29) g_solve.A[col] = v;
+            else if (col >= 32 && col < 60) g_solve.B[col - 32] = v;
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// The fused schedule.  PIX bounds the pixels a thread owns at any level;
+// level l's pixel k = c * chunk_l + s * kFusedThreads + thread, s < pix_l.
+template <int PIX>
+__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_constant__ FusedArgs a) {
+    GNState *st = a.st;
+    __shared__ float sRK[9];
+    const unsigned cta = blockIdx.x, nrows = gridDim.x;
+    const int t = (int)threadIdx.x;
+    const bool do_rgb = (a.mode & YAS_TRACK_RGB) != 0, do_icp = (a.mode & YAS_TRACK_ICP) != 0;
+    load_solve_state(st);
+    if (t >= 32 && t < 64) {
+        g_solve.A[t - 32] = 0.0;
+        g_solve.B[t - 32] = 0.0;
+    }
+    const unsigned epoch = __ldcg(&st->epoch);
+    __syncthreads();
+    unsigned s = 0u;
+    bool alive = true;
+    for (int l = a.L - 1; l >= 0 && alive; --l) {
+        const FusedLevel &lv = a.lv[l];
+        const int n = lv.c.w * lv.c.h;
+        const int base = (int)cta * lv.chunk;
+        for (int it = 0; it < lv.iters; ++it) {
+            ++s;
+            const unsigned tag = (epoch << 12) | (s & 0xfffu);
+            unsigned long long *rA = a.rows + (size_t)((s & 1u) * 2u + 0u) * kFusedMaxCtas * 32;
+            unsigned long long *rB = a.rows + (size_t)((s & 1u) * 2u + 1u) * kFusedMaxCtas * 32;
+            if (t == 0) make_rkinv(g_solve.Tf, lv.c, sRK);
+            __syncthreads();
+            float acc[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) acc[i] = 0.0f;
+            float4 res[PIX];
+            float3 pp[PIX];
+#pragma unroll
+            for (int q = 0; q < PIX; ++q) {
+                res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                pp[q] = make_float3(0.0f, 0.0f, 1.0f);
+                const int off = q * kFusedThreads + t;
+                const int k = base + off;
+                if (q < lv.pix && off < lv.chunk && k < n)
+                    fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, a.angle_th, a.dist_th, acc, res[q], pp[q]);
+            }
+            fused_publish_row(acc, rA + cta * 32, tag);
+            if (do_rgb) {
+                if (!fold_moments(rA, nrows, tag, st)) return;
+                if (t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
+                __syncthreads();
+                const float th = g_solve.huber_th;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[i] = 0.0f;
+#pragma unroll
+                for (int q = 0; q < PIX; ++q)
+                    if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
+                fused_publish_row(acc, rB + cta * 32, tag);
+            }
+            if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st)) return;
+            if (t < 32) {
+                if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
+                gn_solve(a.mode, 0, it == 0, l);
+            }
+            __syncthreads();
+            if (g_solve.failed != 0) {
+                alive = false;
+                break;
+            }
+        }
+    }
+    if (cta == 0 && t < 32) {
+        publish_solve(st);
+        st->a_sums[t] = g_solve.A[t];
+        st->b_sums[t] = g_solve.B[t];
+    }
 }
 
 // ---------------------------------------------------------------- host side
@@ -714,7 +906,98 @@ void launch_gn_iteration(yas_tracker *tr, int l, bool first_of_level, cudaStream
     launch_passes(tr, l, first_of_level ? 1 : 0, 0, s);
 }
 
+
+template <int PIX>
+static cudaError_t launch_fused_pix(const FusedArgs &a, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, gn_fused<PIX>, a);
+}
+
+// Grid of the fused schedule: every co-resident 1024-thread CTA (one per SM),
+// at most kFusedMaxCtas (the rows the system fold covers).  Level l gives each CTA a
+// chunk of ceil(P_l / grid) pixels rounded up to a warp; `pix` is the smallest
+// compiled pixels-per-thread bound (1, 2 or 4) that covers level 0's chunk.
+// Returns false when none does (the per-iteration launches are used).
+static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
+    if (tr->fused_max_grid[0] < 0) {
+        int dev = 0, sms = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        int nb[3] = {0, 0, 0};
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], gn_fused<1>, kFusedThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], gn_fused<2>, kFusedThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], gn_fused<4>, kFusedThreads, 0);
+        cudaGetLastError();
+        for (int i = 0; i < 3; ++i) tr->fused_max_grid[i] = coop ? std::min(nb[i] * sms, kFusedMaxCtas) : 0;
+    }
+    const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
+    const int pixes[3] = {1, 2, 4};
+    for (int i = 0; i < 3; ++i) {
+        const int g = tr->fused_max_grid[i];
+        if (g <= 0) continue;
+        const long long chunk = ((P0 + g - 1) / g + 31) / 32 * 32;
+        if (chunk <= (long long)kFusedThreads * pixes[i]) {
+            pix = pixes[i];
+            grid = g;
+            return true;
+        }
+    }
+    return false;
+}
+
+static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
+    int pix = 0, grid = 0;
+    if (!tr->use_fused || !fused_plan(tr, pix, grid)) return false;
+    FusedArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int l = 0; l < tr->L; ++l) {
+        FusedLevel &f = a.lv[l];
+        f.c = tr->cam[l];
+        f.iters = tr->iters[l];
+        const long long P = (long long)f.c.w * f.c.h;
+        f.chunk = (int)(((P + grid - 1) / grid + 31) / 32 * 32);
+        f.pix = (f.chunk + kFusedThreads - 1) / kFusedThreads;
+        TrackLevelBufs &cb = tr->curb(l), &rb = tr->refb(l);
+        f.ref_int = rb.intensity;
+        f.ref_invd = rb.invd;
+        f.ref_vmap = rb.vmap;
+        f.ref_nmap = rb.nmap;
+        f.cur_int = cb.intensity;
+        f.cur_gx = tr->gx[l];
+        f.cur_gy = tr->gy[l];
+        f.cur_vmap = cb.vmap;
+        f.cur_nmap = cb.nmap;
+    }
+    a.L = tr->L;
+    a.mode = tr->mode;
+    a.angle_th = tr->angle_th;
+    a.dist_th = tr->dist_th;
+    a.rows = tr->fused_rows;
+    a.st = tr->state;
+    if (tr->hook) tr->hook(tr->hook_ctx, 30);
+    const cudaError_t e = pix == 1 ? launch_fused_pix<1>(a, grid, s)
+                                   : (pix == 2 ? launch_fused_pix<2>(a, grid, s) : launch_fused_pix<4>(a, grid, s));
+    if (e != cudaSuccess) {
+        // e.g. a device without cooperative launch: use the per-iteration launches
+        cudaGetLastError();
+        tr->use_fused = false;
+        return false;
+    }
+    return true;
+}
+
 void launch_gn_schedule(yas_tracker *tr, cudaStream_t s) {
+    if (launch_gn_fused(tr, s)) return;
     for (int l = tr->L - 1; l >= 0; --l)
         for (int it = 0; it < tr->iters[l]; ++it) launch_gn_iteration(tr, l, it == 0, s);
 }
@@ -752,10 +1035,11 @@ int tracker_alloc(yas_tracker *tr) {
     tr->growA = (float *)grab((size_t)(kMaxCtas / kGroup) * 64 * 4);
     tr->growB = (float *)grab((size_t)(kMaxCtas / kGroup) * 64 * 4);
     tr->counters = (unsigned *)grab((size_t)2 * (kMaxCtas / kGroup + 1) * 4);
+    tr->fused_rows = (unsigned long long *)grab((size_t)4 * kFusedMaxCtas * 32 * sizeof(unsigned long long));
     tr->state = (GNState *)grab(sizeof(GNState));
     tr->staging_bytes = (size_t)tr->w * tr->h * 4;
     tr->staging = grab(tr->staging_bytes);
-    if (!tr->res4 || !tr->partialA || !tr->partialB || !tr->growA || !tr->growB || !tr->counters || !tr->state || !tr->staging)
+    if (!tr->res4 || !tr->partialA || !tr->partialB || !tr->growA || !tr->growB || !tr->counters || !tr->fused_rows || !tr->state || !tr->staging)
         return YAS_ERR_OOM;
     if (cudaMallocHost(&tr->state_host, sizeof(GNState)) != cudaSuccess) {
         cudaGetLastError();

@@ -19,6 +19,11 @@ struct LevelCam {
     int w, h;
 };
 
+// GNState::failed values: a NaN update, or a bounded wait of the fused
+// schedule that gave up.
+constexpr int kFailNumeric = 1;
+constexpr int kFailTimeout = 3;
+
 // Gauss-Newton state, device resident; written only by the last CTA of a pass.
 struct __align__(16) GNState {
     double est[12];         // current estimate T (reference frame -> current frame)
@@ -39,6 +44,8 @@ struct __align__(16) GNState {
     double b[6];
     double stats[4];        // residualSum, numResidual, huber_th, icp count
     double last_update[6];
+    unsigned epoch;         // launches of the fused schedule (row tags)
+    unsigned abort_word;    // set when a bounded wait of the fused schedule gave up
 };
 
 struct TrackLevelBufs {
@@ -78,6 +85,9 @@ struct yas_tracker {
     float *growA = nullptr;       // per-group (hi, lo) rows of pass A
     float *growB = nullptr;       // per-group (hi, lo) rows of pass B
     unsigned *counters = nullptr; // tickets: pass A grid + groups, then pass B grid + groups
+    unsigned long long *fused_rows = nullptr;  // fused schedule: tagged per-CTA rows
+    bool use_fused = true;        // one cooperative launch for the whole schedule
+    int fused_max_grid[3] = {-1, -1, -1};  // co-resident CTAs for 1, 2, 4 pixels per thread
     yas::GNState *state = nullptr;
     yas::GNState *state_host = nullptr;  // pinned
     void *staging = nullptr;             // host-input staging (w*h*4 bytes)

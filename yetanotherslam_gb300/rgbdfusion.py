@@ -327,6 +327,10 @@ class RGBDTracking:
     def SwapFrameBuffer(self) -> None:
         L.call("yas_tracker_swap_frame_buffer", self.handle)
 
+    def set_schedule(self, fused: bool) -> None:
+        """Whole schedule in one cooperative launch (True) or two launches per iteration."""
+        L.call("yas_tracker_set_schedule", self.handle, int(fused))
+
     def IsTrackingGood(self) -> bool:
         out = C.c_int()
         L.call("yas_tracker_is_good", self.handle, C.byref(out))
@@ -355,7 +359,8 @@ class Session:
     def __init__(self, width: int, height: int, K, hash_slots: int = 1 << 20, max_blocks: int = 1 << 17,
                  voxel_size: float = 0.008, trunc_dist: float | None = None, voxel_format: int = VOXEL_F16,
                  num_levels: int = 3, iterations=(10, 5, 3, 3, 3), mode: int = TRACK_RGBD,
-                 depth_scale: float = 0.001, use_graph: bool = True, stream: int | None = None):
+                 depth_scale: float = 0.001, use_graph: bool = True, stream: int | None = None,
+                 fused_schedule: bool = True):
         cfg = L.SessionConfig()
         trunc = 3 * voxel_size if trunc_dist is None else trunc_dist
         L.call("yas_session_config_default", C.byref(cfg), width, height, C.byref(_intr(K)), hash_slots,
@@ -366,6 +371,7 @@ class Session:
         cfg.mode = mode
         cfg.depth_scale = depth_scale
         cfg.use_graph = int(use_graph)
+        cfg.fused_schedule = int(fused_schedule)
         self.cfg = cfg
         self.width, self.height = width, height
         self.handle = C.c_void_p()
