@@ -194,107 +194,139 @@ struct VoxelReader {
     }
 };
 
+// State of one ray of the march (RayTraceEngine.cu:331-410), in voxel units.
+struct RayState {
+    float3 r, dir, idir;
+    float dist_s, dist_e, sdf;
+    bool valid;
+    unsigned long long skipped;
+};
+
+// Ray of pixel (x, y) between the tile's z-range bounds zn..zf; false when the
+// tile has no range (the pixel is a miss).
+__device__ __forceinline__ bool ray_setup(const Cam &cam, const Rigid32 &T, float vsinv, float zn, float zf, int x,
+                                          int y, RayState &R) {
+    if (zn < FLT_EPSILON || zf < FLT_EPSILON || isnan(zn) || isnan(zf)) return false;
+    const float ux = cam.invfx * ((float)x - cam.cx), uy = cam.invfy * ((float)y - cam.cy);
+    const float3 pn = make_float3(ux * zn, uy * zn, zn);
+    R.dist_s = sqrtf(pn.x * pn.x + pn.y * pn.y + pn.z * pn.z) * vsinv;
+    float3 s = rigid_fast(T, pn.x, pn.y, pn.z);
+    s = make_float3(s.x * vsinv, s.y * vsinv, s.z * vsinv);
+    const float3 pf = make_float3(ux * zf, uy * zf, zf);
+    R.dist_e = sqrtf(pf.x * pf.x + pf.y * pf.y + pf.z * pf.z) * vsinv;
+    float3 e = rigid_fast(T, pf.x, pf.y, pf.z);
+    e = make_float3(e.x * vsinv, e.y * vsinv, e.z * vsinv);
+    float3 dir = make_float3(e.x - s.x, e.y - s.y, e.z - s.z);
+    const float dn = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+    if (dn > 0.0f) dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
+    R.r = s;
+    R.dir = dir;
+    R.idir = make_float3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f,
+                         dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+    R.skipped = kEmptyKey;
+    R.sdf = 1.0f;
+    R.valid = false;
+    return true;
+}
+
+// One iteration of the march loop; true once the ray is finished (a sample
+// with sdf <= 0, or the end of its range).
+template <int FMT>
+__device__ __forceinline__ bool ray_step(VoxelReader<FMT> &rd, float rstep, RayState &R) {
+    if (!(R.dist_s < R.dist_e)) return true;
+    R.sdf = rd.read_nearest(R.r, R.valid);
+    if (rd.cptr < 0 && rd.ckey != R.skipped) {
+        // Unallocated block: every sample until the ray leaves it reads
+        // "unobserved" and advances one voxel, so those samples are skipped in
+        // one move.  k = steps to the first sample outside the block on the
+        // earliest exit axis; two are kept as margin against rounding, so the
+        // samples evaluated next are the last ones inside the block (evaluated
+        // normally).
+        R.skipped = rd.ckey;
+        const float bx0 = floorf(floorf(R.r.x) * 0.125f) * 8.0f;
+        const float by0 = floorf(floorf(R.r.y) * 0.125f) * 8.0f;
+        const float bz0 = floorf(floorf(R.r.z) * 0.125f) * 8.0f;
+        const float kx = R.dir.x > 0.0f ? ceilf((bx0 + 8.0f - R.r.x) * R.idir.x)
+                                        : (R.dir.x < 0.0f ? floorf((bx0 - R.r.x) * R.idir.x) + 1.0f : 1e30f);
+        const float ky = R.dir.y > 0.0f ? ceilf((by0 + 8.0f - R.r.y) * R.idir.y)
+                                        : (R.dir.y < 0.0f ? floorf((by0 - R.r.y) * R.idir.y) + 1.0f : 1e30f);
+        const float kz = R.dir.z > 0.0f ? ceilf((bz0 + 8.0f - R.r.z) * R.idir.z)
+                                        : (R.dir.z < 0.0f ? floorf((bz0 - R.r.z) * R.idir.z) + 1.0f : 1e30f);
+        const float n = fminf(fminf(fminf(kx, ky), kz) - 2.0f, ceilf(R.dist_e - R.dist_s));
+        if (n >= 1.0f) {
+            R.r.x += n * R.dir.x;
+            R.r.y += n * R.dir.y;
+            R.r.z += n * R.dir.z;
+            R.dist_s += n;
+            return false;
+        }
+    }
+    if (R.sdf <= 0.5f && R.sdf >= -0.5f) R.sdf = rd.read_interp(R.r, R.valid);
+    if (R.sdf <= 0.0f) return true;
+    const float step = R.valid ? fmaxf(R.sdf * rstep, 1.0f) : 1.0f;
+    R.r.x += step * R.dir.x;
+    R.r.y += step * R.dir.y;
+    R.r.z += step * R.dir.z;
+    R.dist_s += step;
+    return false;
+}
+
+// Vertex of a finished ray: a hit takes two interpolated correction steps
+// and is returned in camera coordinates (w = 1); a miss is NaN with w = -1.
+template <int FMT>
+__device__ __forceinline__ float4 ray_finish(VoxelReader<FMT> &rd, float rstep, float vsinv, const Rigid32 &Ti,
+                                             RayState &R) {
+    float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                             -1.0f);
+    if (R.sdf <= 0.0f) {
+        float step = R.sdf * rstep;
+        R.r.x += step * R.dir.x;
+        R.r.y += step * R.dir.y;
+        R.r.z += step * R.dir.z;
+        R.sdf = rd.read_interp(R.r, R.valid);
+        step = R.sdf * rstep;
+        R.r.x += step * R.dir.x;
+        R.r.y += step * R.dir.y;
+        R.r.z += step * R.dir.z;
+        if (R.valid) {
+            const float3 w = make_float3(R.r.x / vsinv, R.r.y / vsinv, R.r.z / vsinv);
+            const float3 c = rigid_fast(Ti, w.x, w.y, w.z);
+            out = make_float4(c.x, c.y, c.z, 1.0f);
+        }
+    }
+    return out;
+}
+
+// One thread per pixel; a CTA covers 16x8 pixels, each warp a compact 8x4
+// tile, so its rays travel similar depths.
 template <int FMT>
 __global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const PosePair *P,
                                                     const float *__restrict__ znear,
-                                                    const float *__restrict__ zfar, int zw,
-                                                    float4 *vmap, int vpitch, const int *skip) {
-    // a CTA covers 16x8 pixels; each warp a compact 8x4 tile, so its rays
-    // travel similar depths (less divergence than a 32x1 row)
+                                                    const float *__restrict__ zfar, int zw, float4 *vmap,
+                                                    int vpitch, const int *skip) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
     if (x >= cam.w || y >= cam.h) return;
-    float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
-                             __int_as_float(0x7fffffff), -1.0f);
-    if (skip && *skip) {
-        vmap[(size_t)y * vpitch + x] = out;
-        return;
-    }
-    const float zn = __ldg(znear + (y >> 3) * zw + (x >> 3));
-    const float zf = __ldg(zfar + (y >> 3) * zw + (x >> 3));
-    if (!(zn < FLT_EPSILON || zf < FLT_EPSILON || isnan(zn) || isnan(zf))) {
-        const Rigid32 T = P->T;
+    float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                             -1.0f);
+    if (!(skip && *skip)) {
         const float vsinv = 1.0f / m.voxel_size;
         const float rstep = m.trunc / m.voxel_size;
-        const float ux = cam.invfx * ((float)x - cam.cx), uy = cam.invfy * ((float)y - cam.cy);
-        float3 pn = make_float3(ux * zn, uy * zn, zn);
-        float dist_s = sqrtf(pn.x * pn.x + pn.y * pn.y + pn.z * pn.z) * vsinv;
-        float3 s = rigid_fast(T, pn.x, pn.y, pn.z);
-        s = make_float3(s.x * vsinv, s.y * vsinv, s.z * vsinv);
-        float3 pf = make_float3(ux * zf, uy * zf, zf);
-        const float dist_e = sqrtf(pf.x * pf.x + pf.y * pf.y + pf.z * pf.z) * vsinv;
-        float3 e = rigid_fast(T, pf.x, pf.y, pf.z);
-        e = make_float3(e.x * vsinv, e.y * vsinv, e.z * vsinv);
-        float3 dir = make_float3(e.x - s.x, e.y - s.y, e.z - s.z);
-        float dn = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
-        if (dn > 0.0f) dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
-        float3 r = s;
-        const float3 idir = make_float3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f,
-                                        dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
-        unsigned long long skipped = kEmptyKey;
-        VoxelReader<FMT> rd(m);
-        float sdf = 1.0f;
-        bool valid = false;
-        while (dist_s < dist_e) {
-            sdf = rd.read_nearest(r, valid);
-            if (rd.cptr < 0 && rd.ckey != skipped) {
-                // Unallocated block: every sample until the ray leaves it reads
-                // "unobserved" and advances one voxel, so those samples are
-                // skipped in one move.  k = steps to the first sample outside
-                // the block on the earliest exit axis; two are kept as margin
-                // against rounding, so the samples evaluated next are the last
-                // ones inside the block (evaluated normally).
-                skipped = rd.ckey;
-                const float bx0 = floorf(floorf(r.x) * 0.125f) * 8.0f;
-                const float by0 = floorf(floorf(r.y) * 0.125f) * 8.0f;
-                const float bz0 = floorf(floorf(r.z) * 0.125f) * 8.0f;
-                const float kx = dir.x > 0.0f ? ceilf((bx0 + 8.0f - r.x) * idir.x)
-                                              : (dir.x < 0.0f ? floorf((bx0 - r.x) * idir.x) + 1.0f : 1e30f);
-                const float ky = dir.y > 0.0f ? ceilf((by0 + 8.0f - r.y) * idir.y)
-                                              : (dir.y < 0.0f ? floorf((by0 - r.y) * idir.y) + 1.0f : 1e30f);
-                const float kz = dir.z > 0.0f ? ceilf((bz0 + 8.0f - r.z) * idir.z)
-                                              : (dir.z < 0.0f ? floorf((bz0 - r.z) * idir.z) + 1.0f : 1e30f);
-                const float n = fminf(fminf(fminf(kx, ky), kz) - 2.0f, ceilf(dist_e - dist_s));
-                if (n >= 1.0f) {
-                    r.x += n * dir.x;
-                    r.y += n * dir.y;
-                    r.z += n * dir.z;
-                    dist_s += n;
-                    continue;
-                }
+        RayState R;
+        if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)), __ldg(zfar + (y >> 3) * zw + (x >> 3)),
+                      x, y, R)) {
+            VoxelReader<FMT> rd(m);
+            while (!ray_step(rd, rstep, R)) {
             }
-            if (sdf <= 0.5f && sdf >= -0.5f) sdf = rd.read_interp(r, valid);
-            if (sdf <= 0.0f) break;
-            float step = valid ? fmaxf(sdf * rstep, 1.0f) : 1.0f;
-            r.x += step * dir.x;
-            r.y += step * dir.y;
-            r.z += step * dir.z;
-            dist_s += step;
-        }
-        if (sdf <= 0.0f) {
-            float step = sdf * rstep;
-            r.x += step * dir.x;
-            r.y += step * dir.y;
-            r.z += step * dir.z;
-            sdf = rd.read_interp(r, valid);
-            step = sdf * rstep;
-            r.x += step * dir.x;
-            r.y += step * dir.y;
-            r.z += step * dir.z;
-            if (valid) {
-                const Rigid32 Ti = P->Tinv;
-                float3 w = make_float3(r.x / vsinv, r.y / vsinv, r.z / vsinv);
-                float3 c = rigid_fast(Ti, w.x, w.y, w.z);
-                out = make_float4(c.x, c.y, c.z, 1.0f);
-            }
+            out = ray_finish(rd, rstep, vsinv, P->Tinv, R);
         }
     }
     vmap[(size_t)y * vpitch + x] = out;
 }
 
 void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
-                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
+                            float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
     dim3 grid((cam.w + 15) / 16, (cam.h + 7) / 8);
     switch (fmt) {
         case YAS_VOXEL_F32:
@@ -312,7 +344,6 @@ void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, c
     }
 }
 
-// VMapToDepth (ImageProc.cu:262-286): z of valid vertices, else 0.
 __global__ void vmap_to_depth_kernel(const float4 *vmap, int vpitch, float *depth, int dpitch, int w,
                                      int h) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;

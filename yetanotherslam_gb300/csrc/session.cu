@@ -136,6 +136,10 @@ struct yas_session {
     FrameState *fs_host = nullptr;
     int frames = 0;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    // second stream of a tracked frame: the raycast branch runs beside the
+    // pyramids of the new frame (fork/join events, captured as graph branches)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int kernels_per_frame = 0;
     Cam cam;
     // profiling: events recorded between launches of an eager frame
@@ -179,13 +183,11 @@ static void enqueue_first_frame(yas_session *s) {
     cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, s->stream);
 }
 
-static void enqueue_tracked_frame(yas_session *s) {
+// Raycast of the map at the last pose and the model pyramid built from it
+// (Tracking.cpp:164-169): reads the map and the pose pair, writes the
+// reference set's vertex/normal maps only.
+static void enqueue_raycast_branch(yas_session *s, cudaStream_t st) {
     yas_tracker *tr = s->tr;
-    cudaStream_t st = s->stream;
-    prof_mark(s, kStImage);
-    tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, false, st);
-    prof_mark(s, kStDepth);
-    tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, false, st);
     MapDev v = map_view(s->map);
     prof_mark(s, kStZrange);
     launch_zrange(v, s->rc->cam, &s->fs->pp, s->rc->rb, nullptr, st);
@@ -194,6 +196,33 @@ static void enqueue_tracked_frame(yas_session *s) {
                  nullptr, st);
     prof_mark(s, kStModel);
     tracker_model(tr, st);
+}
+
+// Pyramids of the new frame (Tracking.cpp:172-173): read the frame, write the
+// current set and the float depth only.
+static void enqueue_frame_branch(yas_session *s, cudaStream_t st) {
+    yas_tracker *tr = s->tr;
+    prof_mark(s, kStImage);
+    tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, false, st);
+    prof_mark(s, kStDepth);
+    tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, false, st);
+}
+
+static void enqueue_tracked_frame(yas_session *s) {
+    yas_tracker *tr = s->tr;
+    cudaStream_t st = s->stream;
+    if (s->side && !s->profiling) {
+        // the two branches touch disjoint buffers: run them side by side
+        cudaEventRecord(s->ev_fork, st);
+        cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+        enqueue_raycast_branch(s, s->side);
+        enqueue_frame_branch(s, st);
+        cudaEventRecord(s->ev_join, s->side);
+        cudaStreamWaitEvent(st, s->ev_join, 0);
+    } else {
+        enqueue_frame_branch(s, st);
+        enqueue_raycast_branch(s, st);
+    }
     prof_mark(s, kStGnInit);
     launch_gn_init(tr, pose_identity(), st);
     launch_gn_schedule(tr, st);
@@ -304,6 +333,12 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
     if (st == YAS_OK) {
         s->tr->hook = prof_mark;
         s->tr->hook_ctx = s;
+        if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            st = YAS_ERR_CUDA;
+        }
     }
     if (st == YAS_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) st = YAS_ERR_CUDA;
     if (st != YAS_OK) {
@@ -327,6 +362,12 @@ YAS_API int yas_session_destroy(yas_session *s) {
     cudaFree(s->d_depth_m);
     cudaFree(s->fs);
     if (s->fs_host) cudaFreeHost(s->fs_host);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->own_stream) cudaStreamDestroy(s->stream);
     delete s;
     return YAS_OK;
