@@ -321,6 +321,60 @@ YAS_API void *yas_session_stream(yas_session *s);
 YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device,
                                       int *stage_ids, float *stage_ms, int capacity, int *out_count);
 
+/* ---------------------------------------------------------------- served sessions
+ * No counterpart in the reference, which runs one session per process
+ * (FullSystem/src/System.cpp:43-65).  A request server runs the frames of many
+ * sessions with continuous batching: frames submitted while others are on the
+ * GPU join the next batch as soon as their session has no frame in flight;
+ * each batch runs its sessions' per-frame work on their own streams and all
+ * their Gauss-Newton schedules in one launch.  Sessions are admitted by free
+ * HBM.  A session's results do not depend on which other sessions share its
+ * batches. */
+typedef struct yas_server yas_server;
+
+typedef struct yas_server_config {
+    int max_sessions;         /* live sessions at most                               */
+    size_t hbm_reserve_bytes; /* admission: free HBM - session footprint >= this    */
+    int ring_frames;          /* queued frames per session (pinned input ring)      */
+} yas_server_config;
+
+typedef struct yas_served_result {
+    int session;       /* session id                                           */
+    int status;        /* frame status, as yas_session_wait                    */
+    long long frame;   /* frame number within the session (0 = initialising)   */
+    double latency_ms; /* submission to completion                             */
+    yas_pose Tcm;      /* map pose after the frame                             */
+} yas_served_result;
+
+typedef struct yas_server_stats {
+    long long frames;  /* completed frames since the last reset                */
+    long long batches; /* batched GN launches                                  */
+    double mean_batch; /* tracked frames per batch                             */
+    double p50_ms, p99_ms, max_ms; /* per-frame latency                        */
+    double fps;        /* completed frames / (last completion - first submission) */
+} yas_server_stats;
+
+/* Defaults: 64 sessions, 4 GiB reserve, 4 queued frames per session. */
+YAS_API int yas_server_config_default(yas_server_config *cfg);
+/* Starts the server's worker thread on the current device. */
+YAS_API int yas_server_create(yas_server **out, const yas_server_config *cfg);
+/* Stops the worker, waits for the GPU and frees every session. */
+YAS_API int yas_server_destroy(yas_server *srv);
+/* Admits a session (YAS_ERR_OOM: its footprint does not fit the free HBM minus
+ * the reserve; YAS_ERR_CAPACITY: max_sessions live). */
+YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *cfg, int *out_id);
+/* Drops the session's queued frames, waits for its frame in flight, frees it. */
+YAS_API int yas_server_close_session(yas_server *srv, int id);
+/* Queues one frame (host RGB u8 interleaved, depth u16; copied before the call
+ * returns).  YAS_ERR_CAPACITY: the session's input ring is full. */
+YAS_API int yas_server_submit(yas_server *srv, int id, const uint8_t *rgb, const uint16_t *depth);
+/* Takes up to `capacity` completed results, oldest first. */
+YAS_API int yas_server_poll(yas_server *srv, yas_served_result *out, int capacity, int *out_count);
+/* Waits until no frame is queued or in flight (YAS_ERR_TIMEOUT after timeout_s). */
+YAS_API int yas_server_drain(yas_server *srv, double timeout_s);
+YAS_API int yas_server_get_stats(yas_server *srv, yas_server_stats *out);
+YAS_API int yas_server_reset_stats(yas_server *srv);
+
 #ifdef __cplusplus
 }
 #endif

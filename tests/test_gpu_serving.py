@@ -1,0 +1,99 @@
+"""Served sessions (yas_server_*): continuous batching of many sessions' frames.
+
+Bars:
+  * a session's poses are bit-identical alone in the server and in a mix with
+    other sessions of other resolutions (its work does not depend on its
+    batch: fixed CTA share, own rows, own state);
+  * served poses agree with the same sequence run through a standalone
+    session within 1e-5 m / rad (same arithmetic per pixel, another fold
+    order of the partial sums);
+  * a session whose device footprint does not fit the free HBM minus the
+    reserve is not admitted (YAS_ERR_OOM).
+"""
+from __future__ import annotations
+
+import threading
+
+import numpy as np
+import pytest
+
+from tests.helpers import pose_error, sequence
+from yetanotherslam_gb300 import _lib as L
+from yetanotherslam_gb300 import rgbdfusion as rf
+from yetanotherslam_gb300 import serving, synth
+
+pytestmark = pytest.mark.gpu
+
+MAP = dict(hash_slots=1 << 18, max_blocks=1 << 15, voxel_size=0.008, voxel_format=rf.VOXEL_F16)
+
+
+def _serve_alone(seq, W, H):
+    srv = serving.Server(hbm_reserve_bytes=1 << 30)
+    sid = srv.open(W, H, synth.intrinsics(W, H), **MAP)
+    poses = []
+    for rgb, d16, _, _ in seq:
+        assert srv.submit(sid, rgb, d16) == 0
+        srv.drain()
+        (r,) = srv.poll()
+        assert r["status"] == 0 and r["session"] == sid
+        poses.append(r["Tcm"])
+    srv.close()
+    return poses
+
+
+def test_served_session_same_alone_and_in_mix(cuda):
+    W, H, n = 320, 240, 8
+    seq = sequence(3, n, W, H)
+    alone = _serve_alone(seq, W, H)
+
+    # the same session among three others, all submitting concurrently
+    others = [(160, 120, 5), (320, 240, 7), (640, 480, 9)]
+    srv = serving.Server(hbm_reserve_bytes=1 << 30)
+    sid = srv.open(W, H, synth.intrinsics(W, H), **MAP)
+    oids = [(srv.open(w, h, synth.intrinsics(w, h), **MAP), sequence(seed, n, w, h)) for w, h, seed in others]
+    results: dict[int, list] = {}
+
+    def feed(s, frames):
+        for rgb, d16, _, _ in frames:
+            while srv.submit(s, rgb, d16) != 0:  # ring full: retry
+                threading.Event().wait(0.0005)
+
+    threads = [threading.Thread(target=feed, args=(sid, seq))]
+    threads += [threading.Thread(target=feed, args=(o, fr)) for o, fr in oids]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    srv.drain()
+    for r in srv.poll(1024):
+        results.setdefault(r["session"], []).append(r)
+    st = srv.stats()
+    srv.close()
+    mine = sorted(results[sid], key=lambda r: r["frame"])
+    assert [r["frame"] for r in mine] == list(range(n))
+    for r, T in zip(mine, alone):
+        assert r["status"] == 0
+        assert np.array_equal(r["Tcm"], T)
+    for o, _ in oids:
+        assert len(results[o]) == n and all(r["status"] == 0 for r in results[o])
+    assert st["frames"] == 4 * n and st["p99_ms"] > 0.0
+
+
+def test_served_matches_standalone_session(cuda):
+    W, H, n = 320, 240, 8
+    seq = sequence(3, n, W, H)
+    served = _serve_alone(seq, W, H)
+    s = rf.Session(W, H, synth.intrinsics(W, H), **MAP)
+    for (rgb, d16, _, _), T in zip(seq, served):
+        st, Ts = s.process(rgb, d16)
+        assert st == 0
+        dt, dr = pose_error(Ts, T)
+        assert dt <= 1e-5 and dr <= 1e-5, (dt, dr)
+
+
+def test_admission_by_free_hbm(cuda):
+    srv = serving.Server(hbm_reserve_bytes=1 << 50)  # more than any GPU has
+    with pytest.raises(L.YasError) as e:
+        srv.open(320, 240, synth.intrinsics(320, 240), **MAP)
+    assert e.value.code == 2  # YAS_ERR_OOM: not admitted
+    srv.close()

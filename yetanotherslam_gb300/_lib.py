@@ -52,6 +52,20 @@ class SessionConfig(C.Structure):
                 ("fused_schedule", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_sessions", C.c_int), ("hbm_reserve_bytes", C.c_size_t), ("ring_frames", C.c_int)]
+
+
+class ServedResult(C.Structure):
+    _fields_ = [("session", C.c_int), ("status", C.c_int), ("frame", C.c_longlong), ("latency_ms", C.c_double),
+                ("Tcm", Pose)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("frames", C.c_longlong), ("batches", C.c_longlong), ("mean_batch", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double), ("fps", C.c_double)]
+
+
 class GnLevel(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
                 ("cy", C.c_float), ("ref_intensity", C.c_void_p), ("ref_inv_depth", C.c_void_p),
@@ -135,6 +149,16 @@ _SIGS = {
     "yas_session_profile_frame": [_P, _P, _P, _I, _P, _P, _I, _PI],
     "yas_mc_tables": [_P, _P, _P],
     "yas_gn_linearise_static": [C.POINTER(GnLevel), C.POINTER(Pose), _I, _P, _P],
+    "yas_server_config_default": [C.POINTER(ServerConfig)],
+    "yas_server_create": [_PP, C.POINTER(ServerConfig)],
+    "yas_server_destroy": [_P],
+    "yas_server_open_session": [_P, C.POINTER(SessionConfig), _PI],
+    "yas_server_close_session": [_P, _I],
+    "yas_server_submit": [_P, _I, _P, _P],
+    "yas_server_poll": [_P, C.POINTER(ServedResult), _I, _PI],
+    "yas_server_drain": [_P, C.c_double],
+    "yas_server_get_stats": [_P, C.POINTER(ServerStats)],
+    "yas_server_reset_stats": [_P],
 }
 _RESTYPE = {"yas_status_string": C.c_char_p, "yas_version": C.c_char_p, "yas_session_stream": C.c_void_p}
 

@@ -1,0 +1,471 @@
+// server.cu — request server for concurrent SLAM sessions with continuous
+// batching.  No counterpart in the reference, which runs one session
+// (FullSystem/src/System.cpp:43-65 drives Tracking::GrabImageRGBD per frame).
+//
+// Clients submit frames (host RGB + depth) for their session at any time;
+// each frame is copied into the session's pinned input ring.  One worker
+// thread runs the loop:
+//   1. completed frames (session event done) become results, with their
+//      latency from submission to completion;
+//   2. every session with a queued frame and none in flight joins the next
+//      batch, up to the co-resident CTA capacity of the batched GN launch;
+//   3. per session, on its own stream: input copy, then the first half of the
+//      frame (pyramids, raycast, model pyramid; a captured graph); one
+//      batched Gauss-Newton launch for all tracked frames of the batch on the
+//      server's GN stream; per session again: the second half (pose update,
+//      fusion, frame state to the host).
+// A batch is launched while earlier batches are still on the GPU, so frames
+// that arrive meanwhile overlap with them on the device.  Each session keeps
+// its map, pyramids and buffers device resident; a session is admitted only
+// if its estimated device footprint fits the free HBM minus a reserve.
+//
+// A session's computations are the same alone and in any batch: it takes a
+// fixed CTA count in the batched launch and folds only its own rows.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <thread>
+#include <vector>
+
+#include "yas_session.h"
+
+using namespace yas;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_since(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct QueuedFrame {
+    int slot;                   // input ring slot
+    long long index;            // frame number within the session
+    Clock::time_point arrival;  // submission time
+};
+
+struct ServedSession {
+    int id = -1;
+    yas_session *s = nullptr;
+    int w = 0, h = 0;
+    int ring = 0;
+    uint8_t *rgb = nullptr;    // pinned, ring * w * h * 3
+    uint16_t *depth = nullptr; // pinned, ring * w * h
+    std::vector<bool> slot_used;
+    std::deque<QueuedFrame> queue;
+    bool in_flight = false;
+    QueuedFrame cur{};
+    cudaEvent_t ev_pre = nullptr, ev_done = nullptr;
+    long long submitted = 0, completed = 0;
+    bool closing = false;
+};
+
+// Device footprint of a session with this configuration (map, pyramids,
+// tracker scratch, raycaster and frame buffers), for admission.
+size_t session_bytes_estimate(const yas_session_config &c) {
+    const size_t vbytes = c.map.voxel_format == YAS_VOXEL_F32 ? 8 : 4;
+    const size_t map = (size_t)c.map.hash_slots * 16 + (size_t)c.map.max_blocks * (12 + 512 * vbytes);
+    size_t P = 0;
+    for (int l = 0; l < std::max(1, c.num_levels); ++l) P += (size_t)(c.width >> l) * (c.height >> l);
+    const size_t P0 = (size_t)c.width * c.height;
+    const size_t pyramids = 88 * P;                       // two frame sets + gradients
+    const size_t frame = P0 * (16 + 4 + 16 + 4 + 3 + 2 + 4); // residuals, staging, vmap, depth, inputs
+    return map + pyramids + frame + (8u << 20);            // + tracker rows, graphs, small buffers
+}
+
+}  // namespace
+
+struct yas_server {
+    yas_server_config cfg{};
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<ServedSession *> sessions;  // by id; nullptr once closed
+    std::deque<yas_served_result> results;
+    std::vector<double> latencies;          // ms, since the last stats reset
+    long long batches = 0, batched_frames = 0;
+    Clock::time_point first_submit{}, last_done{};
+    bool have_first = false;
+    std::atomic<bool> stop{false};
+    std::thread worker;
+    int worker_error = YAS_OK;
+    // batched GN launch
+    cudaStream_t gn_stream = nullptr;
+    cudaEvent_t ev_gn = nullptr;
+    static constexpr int kDesc = 4;  // descriptor buffers in rotation
+    GNBatchItem *h_items[kDesc] = {}, *d_items[kDesc] = {};
+    unsigned short *h_map[kDesc] = {}, *d_map[kDesc] = {};
+    cudaEvent_t desc_free[kDesc] = {};
+    int desc_next = 0;
+    int capacity = 0;  // co-resident CTAs of the batched launch
+    int max_items = 0;
+};
+
+namespace {
+
+// Finished frames become results (caller holds the lock).  Returns true if
+// any frame finished.
+bool collect_done(yas_server *srv) {
+    bool any = false;
+    for (ServedSession *ss : srv->sessions) {
+        if (!ss || !ss->in_flight) continue;
+        const cudaError_t q = cudaEventQuery(ss->ev_done);
+        if (q == cudaErrorNotReady) continue;
+        const Clock::time_point now = Clock::now();
+        yas_served_result r;
+        memset(&r, 0, sizeof(r));
+        r.session = ss->id;
+        r.frame = ss->cur.index;
+        r.latency_ms = ms_since(ss->cur.arrival, now);
+        if (q == cudaSuccess) {
+            session_result(ss->s, &r.Tcm, &r.status);
+        } else {
+            record_cuda_error(q, "served frame", __FILE__, __LINE__);
+            r.status = YAS_ERR_CUDA;
+        }
+        if (srv->results.size() >= (1u << 20)) srv->results.pop_front();
+        srv->results.push_back(r);
+        srv->latencies.push_back(r.latency_ms);
+        srv->last_done = now;
+        ss->slot_used[ss->cur.slot] = false;
+        ss->in_flight = false;
+        ss->completed++;
+        any = true;
+    }
+    return any;
+}
+
+int launch_first(ServedSession *ss) {
+    ss->cur = ss->queue.front();
+    ss->queue.pop_front();
+    const size_t n = (size_t)ss->w * ss->h;
+    YAS_TRY(session_copy_input(ss->s, ss->rgb + ss->cur.slot * n * 3, ss->depth + ss->cur.slot * n, 0));
+    YAS_TRY(session_launch_first(ss->s));
+    YAS_TRY_CUDA(cudaEventRecord(ss->ev_done, session_stream(ss->s)));
+    ss->in_flight = true;
+    return YAS_OK;
+}
+
+// One batch of tracked frames: first halves on the session streams, one
+// batched GN launch, second halves on the session streams.
+int launch_batch(yas_server *srv, const std::vector<ServedSession *> &batch) {
+    const int k = srv->desc_next;
+    srv->desc_next = (k + 1) % yas_server::kDesc;
+    // the descriptors of the batch that last used buffer k have been copied
+    YAS_TRY_CUDA(cudaEventSynchronize(srv->desc_free[k]));
+    int cta0 = 0;
+    for (size_t i = 0; i < batch.size(); ++i) {
+        ServedSession *ss = batch[i];
+        ss->cur = ss->queue.front();
+        ss->queue.pop_front();
+        cudaStream_t st = session_stream(ss->s);
+        const size_t n = (size_t)ss->w * ss->h;
+        YAS_TRY(session_copy_input(ss->s, ss->rgb + ss->cur.slot * n * 3, ss->depth + ss->cur.slot * n, 0));
+        YAS_TRY(session_launch_pre(ss->s));
+        GNBatchItem &it = srv->h_items[k][i];
+        gn_batch_item(session_tracker(ss->s), cta0, &it);
+        for (int c = 0; c < it.nctas; ++c) srv->h_map[k][cta0 + c] = (unsigned short)i;
+        cta0 += it.nctas;
+        YAS_TRY_CUDA(cudaEventRecord(ss->ev_pre, st));
+        YAS_TRY_CUDA(cudaStreamWaitEvent(srv->gn_stream, ss->ev_pre, 0));
+    }
+    YAS_TRY_CUDA(cudaMemcpyAsync(srv->d_items[k], srv->h_items[k], batch.size() * sizeof(GNBatchItem),
+                                 cudaMemcpyHostToDevice, srv->gn_stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(srv->d_map[k], srv->h_map[k], (size_t)cta0 * sizeof(unsigned short),
+                                 cudaMemcpyHostToDevice, srv->gn_stream));
+    YAS_TRY_CUDA(cudaEventRecord(srv->desc_free[k], srv->gn_stream));
+    YAS_TRY_CUDA(launch_gn_batch(srv->d_items[k], srv->d_map[k], cta0, srv->gn_stream));
+    YAS_TRY_CUDA(cudaEventRecord(srv->ev_gn, srv->gn_stream));
+    for (ServedSession *ss : batch) {
+        cudaStream_t st = session_stream(ss->s);
+        YAS_TRY_CUDA(cudaStreamWaitEvent(st, srv->ev_gn, 0));
+        YAS_TRY(session_launch_post(ss->s));
+        YAS_TRY_CUDA(cudaEventRecord(ss->ev_done, st));
+        ss->in_flight = true;
+    }
+    srv->batches++;
+    srv->batched_frames += (long long)batch.size();
+    return YAS_OK;
+}
+
+void worker_main(yas_server *srv) {
+    cudaSetDevice(srv->device);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    std::vector<ServedSession *> first, batch;
+    while (!srv->stop.load()) {
+        if (collect_done(srv)) srv->cv.notify_all();
+        first.clear();
+        batch.clear();
+        int ctas = 0;
+        bool busy = false;
+        for (ServedSession *ss : srv->sessions) {
+            if (!ss) continue;
+            busy = busy || ss->in_flight;
+            if (ss->closing || ss->in_flight || ss->queue.empty()) continue;
+            if (session_needs_init(ss->s)) {
+                first.push_back(ss);
+                continue;
+            }
+            const int c = gn_batch_ctas(session_tracker(ss->s));
+            if (ctas + c > srv->capacity || (int)batch.size() >= srv->max_items) continue;
+            ctas += c;
+            batch.push_back(ss);
+        }
+        if (first.empty() && batch.empty()) {
+            if (busy) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                lk.lock();
+            } else {
+                srv->cv.wait_for(lk, std::chrono::milliseconds(2));
+            }
+            continue;
+        }
+        int st = YAS_OK;
+        for (ServedSession *ss : first)
+            if (st == YAS_OK) st = launch_first(ss);
+        if (st == YAS_OK && !batch.empty()) st = launch_batch(srv, batch);
+        if (st != YAS_OK) {
+            srv->worker_error = st;
+            srv->stop.store(true);
+        }
+    }
+    srv->cv.notify_all();
+}
+
+}  // namespace
+
+extern "C" {
+
+YAS_API int yas_server_config_default(yas_server_config *cfg) {
+    if (!cfg) return YAS_ERR_BAD_ARG;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->max_sessions = 64;
+    cfg->hbm_reserve_bytes = (size_t)4 << 30;
+    cfg->ring_frames = 4;
+    return YAS_OK;
+}
+
+YAS_API int yas_server_create(yas_server **out, const yas_server_config *cfg) {
+    if (!out || !cfg || cfg->max_sessions <= 0 || cfg->ring_frames <= 0) return YAS_ERR_BAD_ARG;
+    *out = nullptr;
+    yas_server *srv = new yas_server();
+    srv->cfg = *cfg;
+    cudaGetDevice(&srv->device);
+    srv->capacity = gn_batch_capacity();
+    srv->max_items = std::min(cfg->max_sessions, 1024);
+    bool ok = srv->capacity > 0 &&
+              cudaStreamCreateWithFlags(&srv->gn_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&srv->ev_gn, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; ok && k < yas_server::kDesc; ++k)
+        ok = cudaMallocHost(&srv->h_items[k], srv->max_items * sizeof(GNBatchItem)) == cudaSuccess &&
+             cudaMalloc(&srv->d_items[k], srv->max_items * sizeof(GNBatchItem)) == cudaSuccess &&
+             cudaMallocHost(&srv->h_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
+             cudaMalloc(&srv->d_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
+             cudaEventCreateWithFlags(&srv->desc_free[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        const int code = srv->capacity <= 0 ? YAS_ERR_STATE : YAS_ERR_OOM;
+        yas_server_destroy(srv);
+        return code;
+    }
+    srv->worker = std::thread(worker_main, srv);
+    *out = srv;
+    return YAS_OK;
+}
+
+YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *cfg, int *out_id) {
+    if (!srv || !cfg || !out_id || cfg->width <= 0 || cfg->height <= 0) return YAS_ERR_BAD_ARG;
+    static std::mutex open_mu;  // admission decisions one at a time
+    std::lock_guard<std::mutex> og(open_mu);
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        int live = 0;
+        for (ServedSession *ss : srv->sessions) live += ss ? 1 : 0;
+        if (live >= srv->cfg.max_sessions) return YAS_ERR_CAPACITY;
+    }
+    cudaSetDevice(srv->device);
+    size_t free_b = 0, total_b = 0;
+    YAS_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (free_b < session_bytes_estimate(*cfg) + srv->cfg.hbm_reserve_bytes) return YAS_ERR_OOM;  // not admitted
+    ServedSession *ss = new ServedSession();
+    int st = yas_session_create(&ss->s, cfg, nullptr);
+    ss->w = cfg->width;
+    ss->h = cfg->height;
+    ss->ring = srv->cfg.ring_frames;
+    ss->slot_used.assign(ss->ring, false);
+    const size_t n = (size_t)ss->w * ss->h;
+    if (st == YAS_OK &&
+        (cudaMallocHost(&ss->rgb, ss->ring * n * 3) != cudaSuccess ||
+         cudaMallocHost(&ss->depth, ss->ring * n * 2) != cudaSuccess ||
+         cudaEventCreateWithFlags(&ss->ev_pre, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&ss->ev_done, cudaEventDisableTiming) != cudaSuccess)) {
+        cudaGetLastError();
+        st = YAS_ERR_OOM;
+    }
+    if (st != YAS_OK) {
+        if (ss->s) yas_session_destroy(ss->s);
+        if (ss->rgb) cudaFreeHost(ss->rgb);
+        if (ss->depth) cudaFreeHost(ss->depth);
+        if (ss->ev_pre) cudaEventDestroy(ss->ev_pre);
+        if (ss->ev_done) cudaEventDestroy(ss->ev_done);
+        delete ss;
+        return st;
+    }
+    std::lock_guard<std::mutex> g(srv->mu);
+    ss->id = (int)srv->sessions.size();
+    srv->sessions.push_back(ss);
+    *out_id = ss->id;
+    return YAS_OK;
+}
+
+YAS_API int yas_server_close_session(yas_server *srv, int id) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    ServedSession *ss = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(srv->mu);
+        if (id < 0 || id >= (int)srv->sessions.size() || !srv->sessions[id]) return YAS_ERR_BAD_ARG;
+        ss = srv->sessions[id];
+        ss->closing = true;
+        for (const QueuedFrame &q : ss->queue) ss->slot_used[q.slot] = false;
+        ss->queue.clear();
+        srv->cv.wait(lk, [&] { return !ss->in_flight || srv->stop.load(); });
+        srv->sessions[id] = nullptr;
+    }
+    cudaStreamSynchronize(session_stream(ss->s));
+    yas_session_destroy(ss->s);
+    cudaFreeHost(ss->rgb);
+    cudaFreeHost(ss->depth);
+    cudaEventDestroy(ss->ev_pre);
+    cudaEventDestroy(ss->ev_done);
+    delete ss;
+    return YAS_OK;
+}
+
+YAS_API int yas_server_submit(yas_server *srv, int id, const uint8_t *rgb, const uint16_t *depth) {
+    if (!srv || !rgb || !depth) return YAS_ERR_BAD_ARG;
+    const Clock::time_point arrival = Clock::now();
+    ServedSession *ss = nullptr;
+    int slot = -1;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        if (srv->worker_error != YAS_OK) return srv->worker_error;
+        if (id < 0 || id >= (int)srv->sessions.size() || !srv->sessions[id] || srv->sessions[id]->closing)
+            return YAS_ERR_BAD_ARG;
+        ss = srv->sessions[id];
+        for (int i = 0; i < ss->ring; ++i)
+            if (!ss->slot_used[i]) {
+                slot = i;
+                break;
+            }
+        if (slot < 0) return YAS_ERR_CAPACITY;  // the session's input ring is full
+        ss->slot_used[slot] = true;
+    }
+    const size_t n = (size_t)ss->w * ss->h;
+    memcpy(ss->rgb + slot * n * 3, rgb, n * 3);
+    memcpy(ss->depth + slot * n, depth, n * 2);
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        ss->queue.push_back(QueuedFrame{slot, ss->submitted++, arrival});
+        if (!srv->have_first) {
+            srv->first_submit = arrival;
+            srv->have_first = true;
+        }
+    }
+    srv->cv.notify_all();
+    return YAS_OK;
+}
+
+YAS_API int yas_server_poll(yas_server *srv, yas_served_result *out, int capacity, int *out_count) {
+    if (!srv || !out_count || (capacity > 0 && !out)) return YAS_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    int n = 0;
+    while (n < capacity && !srv->results.empty()) {
+        out[n++] = srv->results.front();
+        srv->results.pop_front();
+    }
+    *out_count = n;
+    return srv->worker_error;
+}
+
+YAS_API int yas_server_drain(yas_server *srv, double timeout_s) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const auto idle = [&] {
+        if (srv->stop.load()) return true;
+        for (ServedSession *ss : srv->sessions)
+            if (ss && (ss->in_flight || !ss->queue.empty())) return false;
+        return true;
+    };
+    if (!srv->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), idle)) return YAS_ERR_TIMEOUT;
+    return srv->worker_error;
+}
+
+YAS_API int yas_server_get_stats(yas_server *srv, yas_server_stats *out) {
+    if (!srv || !out) return YAS_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    memset(out, 0, sizeof(*out));
+    std::vector<double> v = srv->latencies;
+    out->frames = (long long)v.size();
+    out->batches = srv->batches;
+    out->mean_batch = srv->batches ? (double)srv->batched_frames / (double)srv->batches : 0.0;
+    if (!v.empty()) {
+        const auto pct = [&](double p) {
+            size_t i = std::min(v.size() - 1, (size_t)(p * (double)(v.size() - 1) + 0.5));
+            std::nth_element(v.begin(), v.begin() + i, v.end());
+            return v[i];
+        };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        out->max_ms = *std::max_element(v.begin(), v.end());
+        const double span = ms_since(srv->first_submit, srv->last_done);
+        out->fps = span > 0.0 ? 1000.0 * (double)v.size() / span : 0.0;
+    }
+    return YAS_OK;
+}
+
+YAS_API int yas_server_reset_stats(yas_server *srv) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    srv->latencies.clear();
+    srv->batches = 0;
+    srv->batched_frames = 0;
+    srv->have_first = false;
+    return YAS_OK;
+}
+
+YAS_API int yas_server_destroy(yas_server *srv) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    srv->stop.store(true);
+    srv->cv.notify_all();
+    if (srv->worker.joinable()) srv->worker.join();
+    for (size_t i = 0; i < srv->sessions.size(); ++i) {
+        ServedSession *ss = srv->sessions[i];
+        if (!ss) continue;
+        cudaStreamSynchronize(session_stream(ss->s));
+        yas_session_destroy(ss->s);
+        cudaFreeHost(ss->rgb);
+        cudaFreeHost(ss->depth);
+        cudaEventDestroy(ss->ev_pre);
+        cudaEventDestroy(ss->ev_done);
+        delete ss;
+    }
+    if (srv->gn_stream) cudaStreamSynchronize(srv->gn_stream);
+    for (int k = 0; k < yas_server::kDesc; ++k) {
+        if (srv->h_items[k]) cudaFreeHost(srv->h_items[k]);
+        if (srv->d_items[k]) cudaFree(srv->d_items[k]);
+        if (srv->h_map[k]) cudaFreeHost(srv->h_map[k]);
+        if (srv->d_map[k]) cudaFree(srv->d_map[k]);
+        if (srv->desc_free[k]) cudaEventDestroy(srv->desc_free[k]);
+    }
+    if (srv->ev_gn) cudaEventDestroy(srv->ev_gn);
+    if (srv->gn_stream) cudaStreamDestroy(srv->gn_stream);
+    delete srv;
+    return YAS_OK;
+}
+
+}  // extern "C"

@@ -24,7 +24,7 @@
 // YAS_ERR_NUMERIC (the reference fuses at the previous pose).
 #include <cstring>
 
-#include "yas_track.h"
+#include "yas_session.h"
 
 namespace yas {
 
@@ -136,6 +136,8 @@ struct yas_session {
     FrameState *fs_host = nullptr;
     int frames = 0;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraphExec_t pre_exec[2] = {nullptr, nullptr};  // served frames: up to the GN schedule
+    cudaGraphExec_t post_exec = nullptr;               // served frames: after it
     // second stream of a tracked frame: the raycast branch runs beside the
     // pyramids of the new frame (fork/join events, captured as graph branches)
     cudaStream_t side = nullptr;
@@ -208,7 +210,9 @@ static void enqueue_frame_branch(yas_session *s, cudaStream_t st) {
     tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, false, st);
 }
 
-static void enqueue_tracked_frame(yas_session *s) {
+// A tracked frame up to the Gauss-Newton schedule: pyramids of the new frame,
+// raycast of the map and model pyramid, GN state reset.
+static void enqueue_pre(yas_session *s) {
     yas_tracker *tr = s->tr;
     cudaStream_t st = s->stream;
     if (s->side && !s->profiling) {
@@ -225,12 +229,23 @@ static void enqueue_tracked_frame(yas_session *s) {
     }
     prof_mark(s, kStGnInit);
     launch_gn_init(tr, pose_identity(), st);
-    launch_gn_schedule(tr, st);
+}
+
+// A tracked frame after the Gauss-Newton schedule: pose update, fusion, frame
+// state to the host.
+static void enqueue_post(yas_session *s) {
+    cudaStream_t st = s->stream;
     prof_mark(s, kStFinalize);
-    frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, tr->state, s->cfg.max_step_translation, s->map->hdr);
+    frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, s->tr->state, s->cfg.max_step_translation, s->map->hdr);
     enqueue_fusion(s, &s->fs->skip);
     prof_mark(s, kStEnd);
     cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, st);
+}
+
+static void enqueue_tracked_frame(yas_session *s) {
+    enqueue_pre(s);
+    launch_gn_schedule(s->tr, s->stream);
+    enqueue_post(s);
 }
 
 static int count_kernel_nodes(cudaGraph_t g, int *out) {
@@ -248,19 +263,21 @@ static int count_kernel_nodes(cudaGraph_t g, int *out) {
     return YAS_OK;
 }
 
-static int build_graph(yas_session *s, int parity) {
+// Captures `fn` on the session stream into an executable graph; `kernels`
+// (optional) receives its count of kernel nodes.
+static int capture_graph(yas_session *s, void (*fn)(yas_session *), cudaGraphExec_t *out, int *kernels) {
     cudaGraph_t g = nullptr;
     YAS_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_tracked_frame(s);
+    fn(s);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (e != cudaSuccess) {
         record_cuda_error(e, "graph capture", __FILE__, __LINE__);
         if (g) cudaGraphDestroy(g);
         return YAS_ERR_CUDA;
     }
-    int st = count_kernel_nodes(g, &s->kernels_per_frame);
+    int st = kernels ? count_kernel_nodes(g, kernels) : YAS_OK;
     if (st == YAS_OK) {
-        e = cudaGraphInstantiate(&s->exec[parity], g, 0);
+        e = cudaGraphInstantiate(out, g, 0);
         if (e != cudaSuccess) {
             record_cuda_error(e, "graph instantiate", __FILE__, __LINE__);
             st = YAS_ERR_CUDA;
@@ -269,6 +286,56 @@ static int build_graph(yas_session *s, int parity) {
     cudaGraphDestroy(g);
     return st;
 }
+
+static int build_graph(yas_session *s, int parity) {
+    return capture_graph(s, enqueue_tracked_frame, &s->exec[parity], &s->kernels_per_frame);
+}
+
+// ---------------------------------------------------------------- interface for the request server
+namespace yas {
+
+int session_copy_input(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device) {
+    const size_t n = (size_t)s->cfg.width * s->cfg.height;
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->d_depth, depth, n * 2, kind, s->stream));
+    return YAS_OK;
+}
+
+bool session_needs_init(const yas_session *s) { return s->frames == 0; }
+
+int session_launch_first(yas_session *s) {
+    enqueue_first_frame(s);
+    YAS_TRY_CUDA(cudaGetLastError());
+    s->frames++;
+    return YAS_OK;
+}
+
+int session_launch_pre(yas_session *s) {
+    const int parity = s->tr->cur;
+    if (!s->pre_exec[parity]) YAS_TRY(capture_graph(s, enqueue_pre, &s->pre_exec[parity], nullptr));
+    YAS_TRY_CUDA(cudaGraphLaunch(s->pre_exec[parity], s->stream));
+    return YAS_OK;
+}
+
+int session_launch_post(yas_session *s) {
+    if (!s->post_exec) YAS_TRY(capture_graph(s, enqueue_post, &s->post_exec, nullptr));
+    YAS_TRY_CUDA(cudaGraphLaunch(s->post_exec, s->stream));
+    s->tr->cur = 1 - s->tr->cur;
+    s->frames++;
+    return YAS_OK;
+}
+
+yas_tracker *session_tracker(yas_session *s) { return s->tr; }
+cudaStream_t session_stream(yas_session *s) { return s->stream; }
+
+void session_result(const yas_session *s, yas_pose *Tcm, int *status) {
+    if (Tcm)
+        for (int i = 0; i < 12; ++i) Tcm->m[i] = s->fs_host->Tcm[i];
+    if (status) *status = s->fs_host->status;
+}
+
+}  // namespace yas
 
 extern "C" {
 
@@ -352,8 +419,11 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
 YAS_API int yas_session_destroy(yas_session *s) {
     if (!s) return YAS_ERR_BAD_ARG;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < 2; ++i) {
         if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
+    }
+    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
     if (s->tr) yas_tracker_destroy(s->tr);
     if (s->rc) yas_raycaster_destroy(s->rc);
     if (s->map) yas_map_destroy(s->map);

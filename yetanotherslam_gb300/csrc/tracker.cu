@@ -473,16 +473,6 @@ constexpr int kFoldRows = 10;       // rows per subset
 constexpr int kFusedMaxCtas = kFoldSubsets * kFoldRows;  // 160
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
 
-struct FusedLevel {
-    LevelCam c;
-    int iters;
-    int chunk;  // pixels per CTA (a multiple of 32)
-    int pix;    // pixels per thread, ceil(chunk / kFusedThreads)
-    const float *ref_int, *ref_invd;
-    const float4 *ref_vmap, *ref_nmap;
-    const float *cur_int, *cur_gx, *cur_gy;
-    const float4 *cur_vmap, *cur_nmap;
-};
 
 struct FusedArgs {
     FusedLevel lv[kMaxLevels];
@@ -770,15 +760,19 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
     return true;
 }
 
-// The fused schedule.  PIX bounds the pixels a thread owns at any level;
-// level l's pixel k = c * chunk_l + s * kFusedThreads + thread, s < pix_l.
+// The fused schedule of one tracker, run by `nrows` CTAs (this one is `cta`).
+// Level l's pixel k = cta * chunk_l + off, off < chunk_l.  PIX > 0: a thread
+// owns at most PIX pixels per level (off = s * kFusedThreads + thread) and
+// keeps their residuals in registers for pass B; PIX == 0: any number of
+// pixels, residuals through `res4` (pass B then recomputes the warped point,
+// as gn_pass_b does).
 template <int PIX>
-__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_constant__ FusedArgs a) {
-    GNState *st = a.st;
+__device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mode, float angle_th, float dist_th,
+                                            unsigned long long *rows, float4 *res4, GNState *st, unsigned cta,
+                                            unsigned nrows) {
     __shared__ float sRK[9];
-    const unsigned cta = blockIdx.x, nrows = gridDim.x;
     const int t = (int)threadIdx.x;
-    const bool do_rgb = (a.mode & YAS_TRACK_RGB) != 0, do_icp = (a.mode & YAS_TRACK_ICP) != 0;
+    const bool do_rgb = (mode & YAS_TRACK_RGB) != 0, do_icp = (mode & YAS_TRACK_ICP) != 0;
     load_solve_state(st);
     if (t >= 32 && t < 64) {
         g_solve.A[t - 32] = 0.0;
@@ -788,30 +782,41 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_consta
     __syncthreads();
     unsigned s = 0u;
     bool alive = true;
-    for (int l = a.L - 1; l >= 0 && alive; --l) {
-        const FusedLevel &lv = a.lv[l];
+    for (int l = L - 1; l >= 0 && alive; --l) {
+        const FusedLevel &lv = lvs[l];
         const int n = lv.c.w * lv.c.h;
         const int base = (int)cta * lv.chunk;
         for (int it = 0; it < lv.iters; ++it) {
             ++s;
             const unsigned tag = (epoch << 12) | (s & 0xfffu);
-            unsigned long long *rA = a.rows + (size_t)((s & 1u) * 2u + 0u) * kFusedMaxCtas * 32;
-            unsigned long long *rB = a.rows + (size_t)((s & 1u) * 2u + 1u) * kFusedMaxCtas * 32;
+            unsigned long long *rA = rows + (size_t)((s & 1u) * 2u + 0u) * kFusedMaxCtas * 32;
+            unsigned long long *rB = rows + (size_t)((s & 1u) * 2u + 1u) * kFusedMaxCtas * 32;
             if (t == 0) make_rkinv(g_solve.Tf, lv.c, sRK);
             __syncthreads();
             float acc[32];
 #pragma unroll
             for (int i = 0; i < 32; ++i) acc[i] = 0.0f;
-            float4 res[PIX];
-            float3 pp[PIX];
+            float4 res[PIX > 0 ? PIX : 1];
+            float3 pp[PIX > 0 ? PIX : 1];
+            if constexpr (PIX > 0) {
 #pragma unroll
-            for (int q = 0; q < PIX; ++q) {
-                res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-                pp[q] = make_float3(0.0f, 0.0f, 1.0f);
-                const int off = q * kFusedThreads + t;
-                const int k = base + off;
-                if (q < lv.pix && off < lv.chunk && k < n)
-                    fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, a.angle_th, a.dist_th, acc, res[q], pp[q]);
+                for (int q = 0; q < PIX; ++q) {
+                    res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                    pp[q] = make_float3(0.0f, 0.0f, 1.0f);
+                    const int off = q * kFusedThreads + t;
+                    const int k = base + off;
+                    if (q < lv.pix && off < lv.chunk && k < n)
+                        fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, res[q], pp[q]);
+                }
+            } else {
+                for (int off = t; off < lv.chunk; off += kFusedThreads) {
+                    const int k = base + off;
+                    if (k >= n) break;
+                    float4 r4;
+                    float3 p3;
+                    fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, r4, p3);
+                    if (do_rgb) res4[k] = r4;
+                }
             }
             fused_publish_row(acc, rA + cta * 32, tag);
             if (do_rgb) {
@@ -821,15 +826,28 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_consta
                 const float th = g_solve.huber_th;
 #pragma unroll
                 for (int i = 0; i < 32; ++i) acc[i] = 0.0f;
+                if constexpr (PIX > 0) {
 #pragma unroll
-                for (int q = 0; q < PIX; ++q)
-                    if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
+                    for (int q = 0; q < PIX; ++q)
+                        if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
+                } else {
+                    for (int off = t; off < lv.chunk; off += kFusedThreads) {
+                        const int k = base + off;
+                        if (k >= n) break;
+                        const float4 r4 = res4[k];
+                        if (r4.w > 0.0f) {
+                            const int y = k / lv.c.w, x = k - y * lv.c.w;
+                            const float3 p3 = warp_ref_point(sRK, g_solve.Tf, x, y, 1.0f / __ldg(lv.ref_invd + k));
+                            fused_pixel_b(lv.c, th, r4, p3, acc);
+                        }
+                    }
+                }
                 fused_publish_row(acc, rB + cta * 32, tag);
             }
             if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st)) return;
             if (t < 32) {
                 if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
-                gn_solve(a.mode, 0, it == 0, l);
+                gn_solve(mode, 0, it == 0, l);
             }
             __syncthreads();
             if (g_solve.failed != 0) {
@@ -843,6 +861,22 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_consta
         st->a_sums[t] = g_solve.A[t];
         st->b_sums[t] = g_solve.B[t];
     }
+}
+
+// The fused schedule of one tracker over the whole grid.
+template <int PIX>
+__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_constant__ FusedArgs a) {
+    gn_schedule<PIX>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, nullptr, a.st, blockIdx.x, gridDim.x);
+}
+
+// Fused schedules of a batch of trackers in one launch: CTA b runs for item
+// cta_item[b] as its CTA b - cta0 of nctas.  Items never wait on each other,
+// so an item's result is the same alone and in any batch.
+__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused_batch(const GNBatchItem *__restrict__ items,
+                                                                    const unsigned short *__restrict__ cta_item) {
+    const GNBatchItem &it = items[cta_item[blockIdx.x]];
+    gn_schedule<0>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st, blockIdx.x - (unsigned)it.cta0,
+                   (unsigned)it.nctas);
 }
 
 // ---------------------------------------------------------------- host side
@@ -955,13 +989,10 @@ static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
     return false;
 }
 
-static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
-    int pix = 0, grid = 0;
-    if (!tr->use_fused || !fused_plan(tr, pix, grid)) return false;
-    FusedArgs a;
-    memset(&a, 0, sizeof(a));
+// Levels of a fused schedule run by `grid` CTAs, on the tracker's current sets.
+static void fill_levels(yas_tracker *tr, int grid, FusedLevel *lv) {
     for (int l = 0; l < tr->L; ++l) {
-        FusedLevel &f = a.lv[l];
+        FusedLevel &f = lv[l];
         f.c = tr->cam[l];
         f.iters = tr->iters[l];
         const long long P = (long long)f.c.w * f.c.h;
@@ -978,6 +1009,14 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
         f.cur_vmap = cb.vmap;
         f.cur_nmap = cb.nmap;
     }
+}
+
+static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
+    int pix = 0, grid = 0;
+    if (!tr->use_fused || !fused_plan(tr, pix, grid)) return false;
+    FusedArgs a;
+    memset(&a, 0, sizeof(a));
+    fill_levels(tr, grid, a.lv);
     a.L = tr->L;
     a.mode = tr->mode;
     a.angle_th = tr->angle_th;
@@ -994,6 +1033,59 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
         return false;
     }
     return true;
+}
+
+// A tracker takes a fixed number of CTAs in a batch, set by its resolution
+// alone (one per 64 Ki level-0 pixels, 1..16), so its result does not depend
+// on the rest of the batch.
+int gn_batch_ctas(const yas_tracker *tr) {
+    const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
+    return (int)std::min<long long>(16, std::max<long long>(1, (P0 + 65535) / 65536));
+}
+
+void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out) {
+    memset(out, 0, sizeof(*out));
+    out->nctas = gn_batch_ctas(tr);
+    out->cta0 = cta0;
+    fill_levels(tr, out->nctas, out->lv);
+    out->L = tr->L;
+    out->mode = tr->mode;
+    out->angle_th = tr->angle_th;
+    out->dist_th = tr->dist_th;
+    out->rows = tr->fused_rows;
+    out->res4 = tr->res4;
+    out->st = tr->state;
+}
+
+int gn_batch_capacity() {
+    static int cap[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 0;
+    if (cap[dev] == 0) {
+        int sms = 0, nb = 0, coop = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gn_fused_batch, kFusedThreads, 0);
+        cudaGetLastError();
+        cap[dev] = coop ? std::max(0, nb * sms) : -1;
+    }
+    return cap[dev];
+}
+
+cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *dev_cta_item, int grid,
+                            cudaStream_t s) {
+    if (grid <= 0 || grid > gn_batch_capacity()) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, gn_fused_batch, dev_items, dev_cta_item);
 }
 
 void launch_gn_schedule(yas_tracker *tr, cudaStream_t s) {

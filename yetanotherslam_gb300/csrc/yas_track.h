@@ -48,6 +48,31 @@ struct __align__(16) GNState {
     unsigned abort_word;    // set when a bounded wait of the fused schedule gave up
 };
 
+// One pyramid level of a fused Gauss-Newton schedule: camera, iterations,
+// the pixel share of each CTA and the level maps.
+struct FusedLevel {
+    LevelCam c;
+    int iters;
+    int chunk;  // pixels per CTA (a multiple of 32)
+    int pix;    // pixels per thread, ceil(chunk / kFusedThreads)
+    const float *ref_int, *ref_invd;
+    const float4 *ref_vmap, *ref_nmap;
+    const float *cur_int, *cur_gx, *cur_gy;
+    const float4 *cur_vmap, *cur_nmap;
+};
+
+// One tracker's share of a batched Gauss-Newton launch: CTAs cta0 .. cta0 +
+// nctas - 1 run its fused schedule over its own rows and state.
+struct GNBatchItem {
+    FusedLevel lv[kMaxLevels];
+    int L, mode;
+    float angle_th, dist_th;
+    unsigned long long *rows;
+    float4 *res4;
+    GNState *st;
+    int cta0, nctas;
+};
+
 struct TrackLevelBufs {
     float *intensity;
     float *invd;
@@ -120,4 +145,10 @@ void tracker_image(yas_tracker *tr, const uint8_t *src, int channels, int pitch,
 void tracker_depth(yas_tracker *tr, const void *src, int is_u16, int pitch, float scale, float *depth_m,
                    bool reference, cudaStream_t s);
 void tracker_model(yas_tracker *tr, cudaStream_t s);  // model pyramid from ref vmap[0]
+// Batched Gauss-Newton (many trackers, one cooperative launch):
+int gn_batch_ctas(const yas_tracker *tr);               // CTAs a tracker takes in a batch
+void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out);  // descriptor of its current frame
+int gn_batch_capacity();                                // co-resident CTAs of the batched launch
+cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *dev_cta_item, int grid,
+                            cudaStream_t s);
 }  // namespace yas

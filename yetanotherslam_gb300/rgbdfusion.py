@@ -353,6 +353,25 @@ class RGBDTracking:
         return DeviceArray(ptr.value, shape, "<f4", self)
 
 
+def session_config(width: int, height: int, K, hash_slots: int = 1 << 20, max_blocks: int = 1 << 17,
+                   voxel_size: float = 0.008, trunc_dist: float | None = None, voxel_format: int = VOXEL_F16,
+                   num_levels: int = 3, iterations=(10, 5, 3, 3, 3), mode: int = TRACK_RGBD,
+                   depth_scale: float = 0.001, use_graph: bool = True, fused_schedule: bool = True) -> L.SessionConfig:
+    """yas_session_config of a session (the reference's constants unless given)."""
+    cfg = L.SessionConfig()
+    trunc = 3 * voxel_size if trunc_dist is None else trunc_dist
+    L.call("yas_session_config_default", C.byref(cfg), width, height, C.byref(_intr(K)), hash_slots,
+           max_blocks, voxel_size, trunc, voxel_format)
+    cfg.num_levels = num_levels
+    for i in range(5):
+        cfg.iterations[i] = list(iterations)[i] if i < len(iterations) else 0
+    cfg.mode = mode
+    cfg.depth_scale = depth_scale
+    cfg.use_graph = int(use_graph)
+    cfg.fused_schedule = int(fused_schedule)
+    return cfg
+
+
 class Session:
     """One SLAM session's per-frame dense pipeline (Tracking::TrackRGBD's dense calls)."""
 
@@ -361,17 +380,8 @@ class Session:
                  num_levels: int = 3, iterations=(10, 5, 3, 3, 3), mode: int = TRACK_RGBD,
                  depth_scale: float = 0.001, use_graph: bool = True, stream: int | None = None,
                  fused_schedule: bool = True):
-        cfg = L.SessionConfig()
-        trunc = 3 * voxel_size if trunc_dist is None else trunc_dist
-        L.call("yas_session_config_default", C.byref(cfg), width, height, C.byref(_intr(K)), hash_slots,
-               max_blocks, voxel_size, trunc, voxel_format)
-        cfg.num_levels = num_levels
-        for i in range(5):
-            cfg.iterations[i] = list(iterations)[i] if i < len(iterations) else 0
-        cfg.mode = mode
-        cfg.depth_scale = depth_scale
-        cfg.use_graph = int(use_graph)
-        cfg.fused_schedule = int(fused_schedule)
+        cfg = session_config(width, height, K, hash_slots, max_blocks, voxel_size, trunc_dist, voxel_format,
+                             num_levels, iterations, mode, depth_scale, use_graph, fused_schedule)
         self.cfg = cfg
         self.width, self.height = width, height
         self.handle = C.c_void_p()
