@@ -249,6 +249,7 @@ def run_gpu(args):
 
     # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
     cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
+    served = run_served(100 + 1000 * rank) if args.served else None
 
     value = world * args.steps / (total_ms * 1e-3)
     line = {
@@ -278,6 +279,7 @@ def run_gpu(args):
                      "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": round(per_launch[dom], 5),
                      "traffic": traffic},
         "cpu_baseline": cpu,
+        "served": served,
         "clocks": clk.summary(),
     }
     if rank == 0:
@@ -285,6 +287,126 @@ def run_gpu(args):
     s.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+SERVED = {"sessions": 32, "rate_hz": 30.0, "seconds": 3.0, "resolutions": [[640, 480], [320, 240]],
+          "voxel_m": 0.005, "trunc_m": 0.015, "hash_slots": {"640x480": 1 << 21, "320x240": 1 << 20},
+          "max_blocks": 1 << 17, "tsdf": "fp16+u16", "rendered_frames": 30, "saturate_seconds": 1.5}
+
+
+def _pingpong(k: int, n: int) -> int:
+    """Frame k of a back-and-forth walk over n rendered frames (a smooth, endless trajectory)."""
+    period = 2 * (n - 1)
+    k %= period
+    return k if k < n else period - k
+
+
+def run_served(seed: int = 100):
+    """C4: 32 concurrent sessions (half 640x480, half 320x240, distinct seeded scenes), Poisson
+    arrivals at 30 Hz per session, through the request server; then the same sessions saturated
+    (every session resubmits as soon as its ring has room); then the plain FP32 per-frame form
+    (one session, FP32 TSDF, eager launches, per-iteration GN) on the same GPU."""
+    import torch
+
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import serving, synth
+
+    cfg = SERVED
+    n_r = cfg["rendered_frames"]
+    sessions = []
+    for i in range(cfg["sessions"]):
+        W, H = cfg["resolutions"][i % 2]
+        sessions.append((W, H, make_frames(n_r, W, H, seed + i)))
+    srv = serving.Server(max_sessions=cfg["sessions"], hbm_reserve_bytes=8 << 30, ring_frames=8)
+    sids = []
+    for W, H, _ in sessions:
+        sids.append(srv.open(W, H, synth.intrinsics(W, H), hash_slots=cfg["hash_slots"][f"{W}x{H}"],
+                             max_blocks=cfg["max_blocks"], voxel_size=cfg["voxel_m"], trunc_dist=cfg["trunc_m"],
+                             voxel_format=rf.VOXEL_F16, num_levels=3, iterations=(10, 5, 3)))
+    nxt = [0] * len(sids)
+
+    def submit(i):
+        W, H, fr = sessions[i]
+        f = fr[_pingpong(nxt[i], n_r)]
+        code = srv.submit(sids[i], f.rgb, f.depth)
+        if code == 0:
+            nxt[i] += 1
+        return code
+
+    # warm-up: the initialising frame and two tracked frames per session (graph capture)
+    for _ in range(3):
+        for i in range(len(sids)):
+            submit(i)
+        srv.drain(60.0)
+    srv.poll(1 << 16)
+    srv.reset_stats()
+    # Poisson arrivals
+    rng = np.random.default_rng(seed)
+    events = []
+    for i in range(len(sids)):
+        t = rng.exponential(1.0 / cfg["rate_hz"])
+        while t < cfg["seconds"]:
+            events.append((t, i))
+            t += rng.exponential(1.0 / cfg["rate_hz"])
+    events.sort()
+    dropped = 0
+    t0 = time.perf_counter()
+    for t, i in events:
+        while True:
+            now = time.perf_counter() - t0
+            if now >= t:
+                break
+            if t - now > 0.002:
+                time.sleep(t - now - 0.001)
+        if submit(i) != 0:
+            dropped += 1
+    srv.drain(60.0)
+    res = srv.poll(1 << 16)
+    st = srv.stats()
+    bad = sum(1 for r in res if r["status"] != 0)
+    poisson = {"frames": int(st["frames"]), "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+               "max_ms": round(st["max_ms"], 3), "fps": round(st["fps"], 1), "mean_batch": round(st["mean_batch"], 2),
+               "dropped_ring_full": dropped, "frame_status_nonzero": bad}
+    # saturated: keep every session's ring full
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < cfg["saturate_seconds"]:
+        for i in range(len(sids)):
+            submit(i)
+    srv.drain(60.0)
+    srv.poll(1 << 16)
+    sat = srv.stats()
+    srv.close()
+    # plain FP32 per-frame form on the same mix: standalone sessions (FP32 TSDF, eager launches,
+    # two launches per GN iteration), one frame at a time, alternating 640x480 and 320x240
+    plains = []
+    for i in range(4):
+        W, H, fr = sessions[i]
+        p = rf.Session(W, H, synth.intrinsics(W, H), hash_slots=cfg["hash_slots"][f"{W}x{H}"],
+                       max_blocks=cfg["max_blocks"], voxel_size=cfg["voxel_m"], trunc_dist=cfg["trunc_m"],
+                       voxel_format=rf.VOXEL_F32, num_levels=3, iterations=(10, 5, 3), use_graph=False,
+                       fused_schedule=False)
+        dev = [(torch.from_numpy(f.rgb).cuda(), torch.from_numpy(f.depth.view(np.int16)).cuda()) for f in fr]
+        plains.append((p, dev))
+    torch.cuda.synchronize()
+    for k in range(3):
+        for p, dev in plains:
+            p.process(*dev[k])
+    n_plain = 0
+    t0 = time.perf_counter()
+    for k in range(3, n_r):
+        for p, dev in plains:
+            p.process(*dev[k])
+            n_plain += 1
+    plain_fps = n_plain / (time.perf_counter() - t0)
+    for p, _ in plains:
+        p.close()
+    return {"config": {k: v for k, v in cfg.items()}, "poisson": poisson,
+            "saturated": {"frames": int(sat["frames"]), "fps": round(sat["fps"], 1),
+                          "p50_ms": round(sat["p50_ms"], 3), "p99_ms": round(sat["p99_ms"], 3),
+                          "mean_batch": round(sat["mean_batch"], 2)},
+            "plain_fp32_per_frame_fps": round(plain_fps, 1), "plain_mix": "640x480 and 320x240 alternating",
+            "served_over_plain": round(sat["fps"] / plain_fps, 2)}
 
 
 def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
@@ -352,6 +474,7 @@ def main():
     ap.add_argument("--impl", default="yas", choices=["yas", "reference"])
     ap.add_argument("--profile-frames", type=int, default=4)
     ap.add_argument("--cpu-frames", type=int, default=8)
+    ap.add_argument("--served", type=int, default=1, help="1: also measure 32 served sessions (C4)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -41,42 +41,42 @@ def _serve_alone(seq, W, H):
     return poses
 
 
-def test_served_session_same_alone_and_in_mix(cuda):
-    W, H, n = 320, 240, 8
-    seq = sequence(3, n, W, H)
-    alone = _serve_alone(seq, W, H)
+def test_served_sessions_same_alone_and_in_mix(cuda):
+    """Eight sessions of three resolutions submit concurrently (so batches of
+    several sessions form and GN dispatch is deferred while one runs); every
+    session's poses equal, bit for bit, its poses served alone."""
+    n = 8
+    specs = [(320, 240, 3), (160, 120, 5), (320, 240, 7), (640, 480, 9),
+             (160, 120, 11), (640, 480, 13), (320, 240, 15), (160, 120, 17)]
+    seqs = [sequence(seed, n, w, h) for w, h, seed in specs]
+    alone = [_serve_alone(seq, w, h) for (w, h, _), seq in zip(specs, seqs)]
 
-    # the same session among three others, all submitting concurrently
-    others = [(160, 120, 5), (320, 240, 7), (640, 480, 9)]
     srv = serving.Server(hbm_reserve_bytes=1 << 30)
-    sid = srv.open(W, H, synth.intrinsics(W, H), **MAP)
-    oids = [(srv.open(w, h, synth.intrinsics(w, h), **MAP), sequence(seed, n, w, h)) for w, h, seed in others]
-    results: dict[int, list] = {}
+    sids = [srv.open(w, h, synth.intrinsics(w, h), **MAP) for w, h, _ in specs]
 
     def feed(s, frames):
         for rgb, d16, _, _ in frames:
             while srv.submit(s, rgb, d16) != 0:  # ring full: retry
                 threading.Event().wait(0.0005)
 
-    threads = [threading.Thread(target=feed, args=(sid, seq))]
-    threads += [threading.Thread(target=feed, args=(o, fr)) for o, fr in oids]
+    threads = [threading.Thread(target=feed, args=(sid, seq)) for sid, seq in zip(sids, seqs)]
     for t in threads:
         t.start()
     for t in threads:
         t.join()
     srv.drain()
+    results: dict[int, list] = {}
     for r in srv.poll(1024):
         results.setdefault(r["session"], []).append(r)
     st = srv.stats()
     srv.close()
-    mine = sorted(results[sid], key=lambda r: r["frame"])
-    assert [r["frame"] for r in mine] == list(range(n))
-    for r, T in zip(mine, alone):
-        assert r["status"] == 0
-        assert np.array_equal(r["Tcm"], T)
-    for o, _ in oids:
-        assert len(results[o]) == n and all(r["status"] == 0 for r in results[o])
-    assert st["frames"] == 4 * n and st["p99_ms"] > 0.0
+    for sid, ref in zip(sids, alone):
+        mine = sorted(results[sid], key=lambda r: r["frame"])
+        assert [r["frame"] for r in mine] == list(range(n))
+        for r, T in zip(mine, ref):
+            assert r["status"] == 0
+            assert np.array_equal(r["Tcm"], T), (sid, r["frame"])
+    assert st["frames"] == len(specs) * n and st["p99_ms"] > 0.0
 
 
 def test_served_matches_standalone_session(cuda):

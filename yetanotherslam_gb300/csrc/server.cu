@@ -7,15 +7,16 @@
 // thread runs the loop:
 //   1. completed frames (session event done) become results, with their
 //      latency from submission to completion;
-//   2. every session with a queued frame and none in flight joins the next
-//      batch, up to the co-resident CTA capacity of the batched GN launch;
-//   3. per session, on its own stream: input copy, then the first half of the
-//      frame (pyramids, raycast, model pyramid; a captured graph); one
-//      batched Gauss-Newton launch for all tracked frames of the batch on the
-//      server's GN stream; per session again: the second half (pose update,
-//      fusion, frame state to the host).
-// A batch is launched while earlier batches are still on the GPU, so frames
-// that arrive meanwhile overlap with them on the device.  Each session keeps
+//   2. every session with a queued frame and none in flight takes it;
+//   3. a taken frame starts at once on its session's stream: input copy and
+//      the first half of the frame (pyramids, raycast, model pyramid; a
+//      captured graph);
+//   4. whenever fewer than two batched Gauss-Newton launches are pending on
+//      the server's GN stream, every session whose first half is queued joins
+//      one batched launch; the second halves (pose update, fusion, frame
+//      state to the host) follow on the session streams.
+// Frames that arrive while others are on the GPU start at once and their
+// work overlaps with the running batch; under load the batches grow.  Each session keeps
 // its map, pyramids and buffers device resident; a session is admitted only
 // if its estimated device footprint fits the free HBM minus a reserve.
 //
@@ -58,6 +59,7 @@ struct ServedSession {
     std::vector<bool> slot_used;
     std::deque<QueuedFrame> queue;
     bool in_flight = false;
+    bool awaiting_gn = false;  // first half launched, GN not yet dispatched
     QueuedFrame cur{};
     cudaEvent_t ev_pre = nullptr, ev_done = nullptr;
     long long submitted = 0, completed = 0;
@@ -95,11 +97,11 @@ struct yas_server {
     int worker_error = YAS_OK;
     // batched GN launch
     cudaStream_t gn_stream = nullptr;
-    cudaEvent_t ev_gn = nullptr;
     static constexpr int kDesc = 4;  // descriptor buffers in rotation
     GNBatchItem *h_items[kDesc] = {}, *d_items[kDesc] = {};
     unsigned short *h_map[kDesc] = {}, *d_map[kDesc] = {};
-    cudaEvent_t desc_free[kDesc] = {};
+    cudaEvent_t gn_done[kDesc] = {};  // after each buffer's batched GN launch
+    std::deque<int> pending_gn;
     int desc_next = 0;
     int capacity = 0;  // co-resident CTAs of the batched launch
     int max_items = 0;
@@ -112,7 +114,8 @@ namespace {
 bool collect_done(yas_server *srv) {
     bool any = false;
     for (ServedSession *ss : srv->sessions) {
-        if (!ss || !ss->in_flight) continue;
+        // a tracked frame is done only after its second half was launched
+        if (!ss || !ss->in_flight || ss->awaiting_gn) continue;
         const cudaError_t q = cudaEventQuery(ss->ev_done);
         if (q == cudaErrorNotReady) continue;
         const Clock::time_point now = Clock::now();
@@ -150,88 +153,108 @@ int launch_first(ServedSession *ss) {
     return YAS_OK;
 }
 
-// One batch of tracked frames: first halves on the session streams, one
-// batched GN launch, second halves on the session streams.
-int launch_batch(yas_server *srv, const std::vector<ServedSession *> &batch) {
+// First half of a tracked frame on the session's stream, as soon as the
+// frame is taken: input copy, pyramids, raycast, model pyramid, GN reset.
+int launch_pre_frame(ServedSession *ss) {
+    ss->cur = ss->queue.front();
+    ss->queue.pop_front();
+    const size_t n = (size_t)ss->w * ss->h;
+    YAS_TRY(session_copy_input(ss->s, ss->rgb + ss->cur.slot * n * 3, ss->depth + ss->cur.slot * n, 0));
+    YAS_TRY(session_launch_pre(ss->s));
+    YAS_TRY_CUDA(cudaEventRecord(ss->ev_pre, session_stream(ss->s)));
+    ss->in_flight = true;
+    ss->awaiting_gn = true;
+    return YAS_OK;
+}
+
+// One batched Gauss-Newton launch for every session whose first half is
+// queued, then their second halves (pose update, fusion, frame state).
+int dispatch_gn(yas_server *srv, const std::vector<ServedSession *> &batch) {
     const int k = srv->desc_next;
     srv->desc_next = (k + 1) % yas_server::kDesc;
-    // the descriptors of the batch that last used buffer k have been copied
-    YAS_TRY_CUDA(cudaEventSynchronize(srv->desc_free[k]));
+    // buffer k's previous batch has finished (its descriptors were consumed)
+    YAS_TRY_CUDA(cudaEventSynchronize(srv->gn_done[k]));
     int cta0 = 0;
     for (size_t i = 0; i < batch.size(); ++i) {
         ServedSession *ss = batch[i];
-        ss->cur = ss->queue.front();
-        ss->queue.pop_front();
-        cudaStream_t st = session_stream(ss->s);
-        const size_t n = (size_t)ss->w * ss->h;
-        YAS_TRY(session_copy_input(ss->s, ss->rgb + ss->cur.slot * n * 3, ss->depth + ss->cur.slot * n, 0));
-        YAS_TRY(session_launch_pre(ss->s));
         GNBatchItem &it = srv->h_items[k][i];
         gn_batch_item(session_tracker(ss->s), cta0, &it);
         for (int c = 0; c < it.nctas; ++c) srv->h_map[k][cta0 + c] = (unsigned short)i;
         cta0 += it.nctas;
-        YAS_TRY_CUDA(cudaEventRecord(ss->ev_pre, st));
         YAS_TRY_CUDA(cudaStreamWaitEvent(srv->gn_stream, ss->ev_pre, 0));
     }
     YAS_TRY_CUDA(cudaMemcpyAsync(srv->d_items[k], srv->h_items[k], batch.size() * sizeof(GNBatchItem),
                                  cudaMemcpyHostToDevice, srv->gn_stream));
     YAS_TRY_CUDA(cudaMemcpyAsync(srv->d_map[k], srv->h_map[k], (size_t)cta0 * sizeof(unsigned short),
                                  cudaMemcpyHostToDevice, srv->gn_stream));
-    YAS_TRY_CUDA(cudaEventRecord(srv->desc_free[k], srv->gn_stream));
     YAS_TRY_CUDA(launch_gn_batch(srv->d_items[k], srv->d_map[k], cta0, srv->gn_stream));
-    YAS_TRY_CUDA(cudaEventRecord(srv->ev_gn, srv->gn_stream));
+    YAS_TRY_CUDA(cudaEventRecord(srv->gn_done[k], srv->gn_stream));
     for (ServedSession *ss : batch) {
         cudaStream_t st = session_stream(ss->s);
-        YAS_TRY_CUDA(cudaStreamWaitEvent(st, srv->ev_gn, 0));
+        YAS_TRY_CUDA(cudaStreamWaitEvent(st, srv->gn_done[k], 0));
         YAS_TRY(session_launch_post(ss->s));
         YAS_TRY_CUDA(cudaEventRecord(ss->ev_done, st));
-        ss->in_flight = true;
+        ss->awaiting_gn = false;
     }
+    srv->pending_gn.push_back(k);
     srv->batches++;
     srv->batched_frames += (long long)batch.size();
     return YAS_OK;
 }
 
+// Batched GN launches not yet finished (caller holds the lock).
+int pending_gn(yas_server *srv) {
+    while (!srv->pending_gn.empty() && cudaEventQuery(srv->gn_done[srv->pending_gn.front()]) == cudaSuccess)
+        srv->pending_gn.pop_front();
+    return (int)srv->pending_gn.size();
+}
+
 void worker_main(yas_server *srv) {
     cudaSetDevice(srv->device);
     std::unique_lock<std::mutex> lk(srv->mu);
-    std::vector<ServedSession *> first, batch;
+    std::vector<ServedSession *> batch;
     while (!srv->stop.load()) {
         if (collect_done(srv)) srv->cv.notify_all();
-        first.clear();
-        batch.clear();
-        int ctas = 0;
-        bool busy = false;
+        int st = YAS_OK;
+        bool launched = false, busy = false;
+        // every session with a queued frame and none in flight starts it now
         for (ServedSession *ss : srv->sessions) {
             if (!ss) continue;
+            if (!ss->closing && !ss->in_flight && !ss->queue.empty() && st == YAS_OK) {
+                st = session_needs_init(ss->s) ? launch_first(ss) : launch_pre_frame(ss);
+                launched = true;
+            }
             busy = busy || ss->in_flight;
-            if (ss->closing || ss->in_flight || ss->queue.empty()) continue;
-            if (session_needs_init(ss->s)) {
-                first.push_back(ss);
-                continue;
-            }
-            const int c = gn_batch_ctas(session_tracker(ss->s));
-            if (ctas + c > srv->capacity || (int)batch.size() >= srv->max_items) continue;
-            ctas += c;
-            batch.push_back(ss);
         }
-        if (first.empty() && batch.empty()) {
-            if (busy) {
-                lk.unlock();
-                std::this_thread::sleep_for(std::chrono::microseconds(20));
-                lk.lock();
-            } else {
-                srv->cv.wait_for(lk, std::chrono::milliseconds(2));
+        // the waiting sessions form the next GN batch once fewer than two
+        // batches are on the GN stream (while one runs, the next gathers)
+        if (st == YAS_OK && pending_gn(srv) < 2) {
+            batch.clear();
+            int ctas = 0;
+            for (ServedSession *ss : srv->sessions) {
+                if (!ss || !ss->awaiting_gn) continue;
+                const int c = gn_batch_ctas(session_tracker(ss->s));
+                if (ctas + c > srv->capacity || (int)batch.size() >= srv->max_items) continue;
+                ctas += c;
+                batch.push_back(ss);
             }
-            continue;
+            if (!batch.empty()) {
+                st = dispatch_gn(srv, batch);
+                launched = true;
+            }
         }
-        int st = YAS_OK;
-        for (ServedSession *ss : first)
-            if (st == YAS_OK) st = launch_first(ss);
-        if (st == YAS_OK && !batch.empty()) st = launch_batch(srv, batch);
         if (st != YAS_OK) {
             srv->worker_error = st;
             srv->stop.store(true);
+            break;
+        }
+        if (launched) continue;
+        if (busy) {
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(10));
+            lk.lock();
+        } else {
+            srv->cv.wait_for(lk, std::chrono::milliseconds(2));
         }
     }
     srv->cv.notify_all();
@@ -258,15 +281,13 @@ YAS_API int yas_server_create(yas_server **out, const yas_server_config *cfg) {
     cudaGetDevice(&srv->device);
     srv->capacity = gn_batch_capacity();
     srv->max_items = std::min(cfg->max_sessions, 1024);
-    bool ok = srv->capacity > 0 &&
-              cudaStreamCreateWithFlags(&srv->gn_stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&srv->ev_gn, cudaEventDisableTiming) == cudaSuccess;
+    bool ok = srv->capacity > 0 && cudaStreamCreateWithFlags(&srv->gn_stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int k = 0; ok && k < yas_server::kDesc; ++k)
         ok = cudaMallocHost(&srv->h_items[k], srv->max_items * sizeof(GNBatchItem)) == cudaSuccess &&
              cudaMalloc(&srv->d_items[k], srv->max_items * sizeof(GNBatchItem)) == cudaSuccess &&
              cudaMallocHost(&srv->h_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
              cudaMalloc(&srv->d_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
-             cudaEventCreateWithFlags(&srv->desc_free[k], cudaEventDisableTiming) == cudaSuccess;
+             cudaEventCreateWithFlags(&srv->gn_done[k], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         const int code = srv->capacity <= 0 ? YAS_ERR_STATE : YAS_ERR_OOM;
@@ -460,9 +481,8 @@ YAS_API int yas_server_destroy(yas_server *srv) {
         if (srv->d_items[k]) cudaFree(srv->d_items[k]);
         if (srv->h_map[k]) cudaFreeHost(srv->h_map[k]);
         if (srv->d_map[k]) cudaFree(srv->d_map[k]);
-        if (srv->desc_free[k]) cudaEventDestroy(srv->desc_free[k]);
+        if (srv->gn_done[k]) cudaEventDestroy(srv->gn_done[k]);
     }
-    if (srv->ev_gn) cudaEventDestroy(srv->ev_gn);
     if (srv->gn_stream) cudaStreamDestroy(srv->gn_stream);
     delete srv;
     return YAS_OK;

@@ -809,6 +809,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                         fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, res[q], pp[q]);
                 }
             } else {
+#pragma unroll 2
                 for (int off = t; off < lv.chunk; off += kFusedThreads) {
                     const int k = base + off;
                     if (k >= n) break;
@@ -831,6 +832,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     for (int q = 0; q < PIX; ++q)
                         if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
                 } else {
+#pragma unroll 2
                     for (int off = t; off < lv.chunk; off += kFusedThreads) {
                         const int k = base + off;
                         if (k >= n) break;
@@ -1036,11 +1038,11 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
 }
 
 // A tracker takes a fixed number of CTAs in a batch, set by its resolution
-// alone (one per 64 Ki level-0 pixels, 1..16), so its result does not depend
+// alone (one per 32 Ki level-0 pixels, 1..16), so its result does not depend
 // on the rest of the batch.
 int gn_batch_ctas(const yas_tracker *tr) {
     const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
-    return (int)std::min<long long>(16, std::max<long long>(1, (P0 + 65535) / 65536));
+    return (int)std::min<long long>(16, std::max<long long>(1, (P0 + 32767) / 32768));
 }
 
 void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out) {
