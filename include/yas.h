@@ -140,6 +140,21 @@ YAS_API int yas_map_reactivate(yas_map *map);
 YAS_API int yas_map_is_hibernated(yas_map *map, int *out);
 /* Device-memory footprint in bytes (tables, pool, lists). */
 YAS_API int yas_map_device_bytes(yas_map *map, size_t *out_bytes);
+/* MapStruct::Reserve(hashTableSize, bucketSize, voxelBlockSize), VoxelMap.cu:479-515:
+ * grows the table to >= hash_slots slots (power of two) and the pool to
+ * >= max_blocks blocks; blocks keep their contents, the table is rebuilt. */
+YAS_API int yas_map_reserve(yas_map *map, int hash_slots, int max_blocks);
+/* MapStruct::Fuse(MapStruct *src), VoxelMap.cu:398-444 (System::FuseAllMapStruct,
+ * System.cpp:73-93): fuses src into map using both maps' poses (yas_map_get_pose);
+ * an empty map takes src's storage and pose.  src is left empty (the reference
+ * releases it); destroy it with yas_map_destroy.  Same voxel size and format. */
+YAS_API int yas_map_fuse_map(yas_map *map, yas_map *src);
+/* No counterpart in the reference: removes the observation of one depth frame
+ * at pose Tcm (the inverse of yas_map_fuse_depth's running average, exact
+ * where that frame was fused and the weight stayed below the cap), for
+ * re-integration after a pose correction. */
+YAS_API int yas_map_defuse_depth(yas_map *map, const float *depth, int width, int height, int pitch_bytes,
+                                 int on_device, const yas_pose *Tcm);
 
 /* ---------------------------------------------------------------- RayTraceEngine
  * Replaces class RayTraceEngine (RGBDFusion/include/RayTraceEngine.h:11-49). */

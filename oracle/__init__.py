@@ -46,6 +46,8 @@ _SIGS = {
     "orc_session_frame": ([_P, _P, _P, _P], _I),
     "orc_session_map": ([_P], _P),
     "orc_session_tracker": ([_P], _P),
+    "orc_map_defuse": ([_P, _P, _I, _I, _P, _P], _I),
+    "orc_map_fuse_map": ([_P, _P, _P, _P], _I),
     "orc_se3_exp": ([_P, _P], None),
     "orc_ldlt_solve6": ([_P, _P, _P], None),
     "orc_real_bytes": ([], _I),
@@ -99,6 +101,15 @@ class Map:
     def fuse(self, depth: np.ndarray, K, Tcm) -> int:
         d = np.ascontiguousarray(depth, dtype=np.float32)
         return self.L.orc_map_fuse(self.h, _ptr(d), d.shape[1], d.shape[0], _ptr(_kvec(K)), _ptr(_pose(Tcm)))
+
+    def defuse(self, depth: np.ndarray, K, Tcm) -> int:
+        d = np.ascontiguousarray(depth, dtype=np.float32)
+        return self.L.orc_map_defuse(self.h, _ptr(d), d.shape[1], d.shape[0], _ptr(_kvec(K)), _ptr(_pose(Tcm)))
+
+    def fuse_map(self, src: "Map", T_self, T_src) -> bool:
+        """MapStruct::Fuse(MapStruct*); True if this map was empty and took src's storage."""
+        a, b = _pose(T_self), _pose(T_src)
+        return bool(self.L.orc_map_fuse_map(self.h, src.h, _ptr(a), _ptr(b)))
 
     def visible(self, cols: int, rows: int, K, Tcm) -> np.ndarray:
         out = np.zeros((max(self.num_blocks, 1), 3), dtype=np.int32)

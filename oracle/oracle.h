@@ -51,6 +51,11 @@ void orc_map_allocate(orc_map *m, const float *depth, int w, int h, const float 
 int orc_map_visible(orc_map *m, int cols, int rows, const float *K, const double *Tcm, int *coords, int cap);
 /* Fuse(depth, Tcm): allocation + visibility + integration; returns #visible. */
 int orc_map_fuse(orc_map *m, const float *depth, int w, int h, const float *K, const double *Tcm);
+/* De-integration of one depth frame (the inverse running-average update). */
+int orc_map_defuse(orc_map *m, const float *depth, int w, int h, const float *K, const double *Tcm);
+/* MapStruct::Fuse(MapStruct*): fuses src into dst (poses: 3x4 world poses of
+ * the two submaps); returns 1 if dst was empty and took src's storage. */
+int orc_map_fuse_map(orc_map *dst, orc_map *src, const double *Tdst, const double *Tsrc);
 /* Block coords (3 ints), sdf and weight (512 each) in insertion order. */
 void orc_map_export(const orc_map *m, int *coords, double *sdf, double *wt);
 /* Inserts/overwrites blocks with given float contents. */

@@ -271,8 +271,10 @@ int orc_map_visible(orc_map *m, int cols, int rows, const float *K, const double
 
 /* Integration (VoxelMap.cu:738-785): pixel selection and gates in FP32, the
  * running weighted average in `real`. */
+/* sign = +1: DepthFusionFunctor (VoxelMap.cu:719-786); sign = -1: the same
+ * observation removed (s <- (s w - d) / (w - 1), w <- w - 1; w = 1 -> unobserved). */
 static void integrate(orc_map *m, const float *depth, int w, int h, const float *K, const double *Tcm, const int *list,
-                      int nvis) {
+                      int nvis, int sign) {
     const rig32 Tinv = rig_inv_from(Tcm);
     const float ntrunc = -m->trunc;
 #ifdef _OPENMP
@@ -300,12 +302,20 @@ static void integrate(orc_map *m, const float *depth, int w, int h, const float 
                     if (sdf > 1) sdf = 1;
                     const size_t k = (size_t)b * 512 + lz * 64 + ly * 8 + lx;
                     const int wt = m->wt[k];
-                    if (wt == 0) {
-                        m->sdf[k] = sdf;
-                        m->wt[k] = 1;
-                    } else {
-                        m->sdf[k] = (m->sdf[k] * (real)wt + sdf) / (real)(wt + 1);
-                        m->wt[k] = wt + 1 < m->max_w ? wt + 1 : m->max_w;
+                    if (sign > 0) {
+                        if (wt == 0) {
+                            m->sdf[k] = sdf;
+                            m->wt[k] = 1;
+                        } else {
+                            m->sdf[k] = (m->sdf[k] * (real)wt + sdf) / (real)(wt + 1);
+                            m->wt[k] = wt + 1 < m->max_w ? wt + 1 : m->max_w;
+                        }
+                    } else if (wt == 1) {
+                        m->sdf[k] = 0;
+                        m->wt[k] = 0;
+                    } else if (wt > 1) {
+                        m->sdf[k] = (m->sdf[k] * (real)wt - sdf) / (real)(wt - 1);
+                        m->wt[k] = wt - 1;
                     }
                 }
     }
@@ -315,7 +325,15 @@ int orc_map_fuse(orc_map *m, const float *depth, int w, int h, const float *K, c
     orc_map_allocate(m, depth, w, h, K, Tcm);
     int *list = (int *)malloc(sizeof(int) * (m->n + 1));
     int n = collect_visible(m, w, h, K, Tcm, list);
-    integrate(m, depth, w, h, K, Tcm, list, n);
+    integrate(m, depth, w, h, K, Tcm, list, n, 1);
+    free(list);
+    return n;
+}
+
+int orc_map_defuse(orc_map *m, const float *depth, int w, int h, const float *K, const double *Tcm) {
+    int *list = (int *)malloc(sizeof(int) * (m->n + 1));
+    int n = collect_visible(m, w, h, K, Tcm, list);
+    integrate(m, depth, w, h, K, Tcm, list, n, -1);
     free(list);
     return n;
 }
@@ -342,6 +360,117 @@ void orc_map_import(orc_map *m, const int *coords, const float *sdf, const float
             m->wt[(size_t)b * 512 + k] = (int)wt[(size_t)i * 512 + k];
         }
     }
+}
+
+/* ------------------------------------------------------------ submap fusion
+ * MapStruct::Fuse(MapStruct*) (VoxelMap.cu:398-444): CreateBlockFunctor
+ * (:231-262), then MapStructFusionFunctor (:363-396) with InterpolateSDF's
+ * corner order and lerps (:305-361).  Poses: the maps' poses in the world
+ * (3x4 row-major); source -> destination = inv(Tdst) Tsrc, composed in double
+ * in the order of the library's host pose algebra and rounded once. */
+static void pose_inv12(const double *T, double *o) {
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) o[i * 4 + j] = T[j * 4 + i];
+        o[i * 4 + 3] = -((T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7]) + T[2 * 4 + i] * T[11]);
+    }
+}
+
+static void pose_mul12(const double *a, const double *b, double *o) {
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            o[i * 4 + j] = (a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j]) + a[i * 4 + 2] * b[2 * 4 + j];
+        o[i * 4 + 3] = ((a[i * 4 + 0] * b[3] + a[i * 4 + 1] * b[7]) + a[i * 4 + 2] * b[11]) + a[i * 4 + 3];
+    }
+}
+
+static real read_voxel_w(const orc_map *m, int vx, int vy, int vz, int *wt) {
+    int b = find_block(m, floor_div8(vx), floor_div8(vy), floor_div8(vz));
+    if (b < 0) {
+        *wt = 0;
+        return 1;
+    }
+    const size_t k = (size_t)b * 512 + ((vz & 7) << 6) + ((vy & 7) << 3) + (vx & 7);
+    *wt = m->wt[k];
+    return *wt ? m->sdf[k] : 1;
+}
+
+static void map_clear(orc_map *m) {
+    m->n = 0;
+    for (int i = 0; i < m->hcap; ++i) m->hkey[i] = EMPTY_KEY;
+}
+
+/* Returns 1 when dst was empty and took src's storage (the caller swaps the
+ * poses), else 0; src is left empty. */
+int orc_map_fuse_map(orc_map *dst, orc_map *src, const double *Tdst, const double *Tsrc) {
+    if (src->n == 0) return 0;
+    if (dst->n == 0) {
+        orc_map t = *dst;
+        *dst = *src;
+        *src = t;
+        return 1;
+    }
+    double inv[12], t_sd[12], t_ds[12];
+    pose_inv12(Tdst, inv);
+    pose_mul12(inv, Tsrc, t_sd);
+    pose_inv12(Tsrc, inv);
+    pose_mul12(inv, Tdst, t_ds);
+    const rig32 A = rig_from(t_sd), B = rig_from(t_ds);
+    const float vs = dst->vs;
+    for (int b = 0; b < src->n; ++b) {
+        const int bx = src->coords[3 * b], by = src->coords[3 * b + 1], bz = src->coords[3 * b + 2];
+        for (int li = 0; li < 512; ++li) {
+            if (src->wt[(size_t)b * 512 + li] == 0) continue;
+            float p[3];
+            rig_apply(&A, (float)(bx * 8 + (li & 7)) * vs, (float)(by * 8 + ((li >> 3) & 7)) * vs,
+                      (float)(bz * 8 + (li >> 6)) * vs, p);
+            insert_block(dst, floor_div8(f2i_floor(p[0] / vs)), floor_div8(f2i_floor(p[1] / vs)),
+                         floor_div8(f2i_floor(p[2] / vs)));
+        }
+    }
+    const int ndst = dst->n;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int b = 0; b < ndst; ++b) {
+        const int bx = dst->coords[3 * b], by = dst->coords[3 * b + 1], bz = dst->coords[3 * b + 2];
+        for (int li = 0; li < 512; ++li) {
+            float p[3];
+            rig_apply(&B, (float)(bx * 8 + (li & 7)) * vs, (float)(by * 8 + ((li >> 3) & 7)) * vs,
+                      (float)(bz * 8 + (li >> 6)) * vs, p);
+            const float qx = p[0] / vs, qy = p[1] / vs, qz = p[2] / vs;
+            const float fx = floorf(qx), fy = floorf(qy), fz = floorf(qz);
+            const int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+            const real ax = (real)(qx - fx), ay = (real)(qy - fy), az = (real)(qz - fz);
+            int w0, w;
+            const real s000 = read_voxel_w(src, x0, y0, z0, &w0);
+            if (!w0) continue;
+            const real s100 = read_voxel_w(src, x0 + 1, y0, z0, &w);
+            if (!w) continue;
+            const real s010 = read_voxel_w(src, x0, y0 + 1, z0, &w);
+            if (!w) continue;
+            const real s110 = read_voxel_w(src, x0 + 1, y0 + 1, z0, &w);
+            if (!w) continue;
+            const real s001 = read_voxel_w(src, x0, y0, z0 + 1, &w);
+            if (!w) continue;
+            const real s101 = read_voxel_w(src, x0 + 1, y0, z0 + 1, &w);
+            if (!w) continue;
+            const real s011 = read_voxel_w(src, x0, y0 + 1, z0 + 1, &w);
+            if (!w) continue;
+            const real s111 = read_voxel_w(src, x0 + 1, y0 + 1, z0 + 1, &w);
+            if (!w) continue;
+            const real r0 = s000 * (1 - ax) + s100 * ax;
+            const real r1 = r0 * (1 - ay) + (s010 * (1 - ax) + s110 * ax) * ay;
+            const real r2 = s001 * (1 - ax) + s101 * ax;
+            const real sv = r1 * (1 - az) + (r2 * (1 - ay) + (s011 * (1 - ax) + s111 * ax) * ay) * az;
+            const size_t k = (size_t)b * 512 + li;
+            const int dw = dst->wt[k];
+            const real ds = dw ? dst->sdf[k] : 0;
+            dst->sdf[k] = (ds * (real)dw + sv * (real)w0) / (real)(dw + w0);
+            dst->wt[k] = dw + w0 < dst->max_w ? dw + w0 : dst->max_w;
+        }
+    }
+    map_clear(src);
+    return 0;
 }
 
 /* ------------------------------------------------------------ raycast */

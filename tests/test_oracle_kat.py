@@ -321,3 +321,42 @@ def _vmap_of(depth, K):
     v[..., 2] = z
     v[..., 3] = np.where((z > 0.2) & (z < 3.0), 1.0, -1.0)
     return v
+
+
+def test_oracle_fuse_map_identity_and_defuse_kat():
+    """Fusing a map into an identical copy at the same pose doubles every
+    weight (below the cap) and keeps every sdf whose eight-voxel cell is fully
+    observed; de-integrating a frame right after fusing it restores the map.
+    The voxel size is a power of two (2^-7 m), so voxel -> metres -> voxel is
+    exact in FP32 and the identity maps every voxel onto itself."""
+    from yetanotherslam_gb300 import synth
+    from tests.helpers import sequence
+
+    W, H = 160, 120
+    K = synth.intrinsics(W, H)
+    seq = sequence(31, 2, W, H)
+    vs = 2.0 ** -7
+    a = oracle.Map(vs, 3 * vs)
+    b = oracle.Map(vs, 3 * vs)
+    for _, _, dm, T in seq:
+        a.fuse(dm, K, T)
+        b.fuse(dm, K, T)
+    ca, sa, wa = a.export()
+    assert not a.fuse_map(b, np.eye(4), np.eye(4))
+    assert b.num_blocks == 0
+    c2, s2, w2 = a.export()
+    assert np.array_equal(ca, c2)
+    moved = w2 != wa
+    assert moved.any()
+    assert np.array_equal(w2[moved], np.minimum(2 * wa[moved], 255))
+    assert np.abs(s2[moved] - sa[moved]).max() < 1e-12
+    d = oracle.Map(vs, 3 * vs)
+    d.fuse(seq[0][2], K, seq[0][3])
+    c0, s0, w0 = d.export()
+    d.fuse(seq[1][2], K, seq[1][3])
+    d.defuse(seq[1][2], K, seq[1][3])
+    c1, s1, w1 = d.export()
+    n0 = c0.shape[0]
+    assert np.array_equal(c1[:n0], c0) and np.array_equal(w1[:n0], w0)
+    obs = w0 > 0
+    assert np.abs(s1[:n0][obs] - s0[obs]).max() < 1e-12

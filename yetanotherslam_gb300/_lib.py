@@ -106,6 +106,9 @@ _SIGS = {
     "yas_map_reactivate": [_P],
     "yas_map_is_hibernated": [_P, _PI],
     "yas_map_device_bytes": [_P, C.POINTER(C.c_size_t)],
+    "yas_map_reserve": [_P, _I, _I],
+    "yas_map_fuse_map": [_P, _P],
+    "yas_map_defuse_depth": [_P, _P, _I, _I, _I, _I, C.POINTER(Pose)],
     "yas_raycaster_create": [_PP, _I, _I, C.POINTER(Intrinsics), _P],
     "yas_raycaster_destroy": [_P],
     "yas_raycaster_raycast": [_P, _P, C.POINTER(Pose)],

@@ -1,6 +1,7 @@
 // capi.cu — extern "C" entry points of libyas_gb300 for the map, raycaster,
 // mesher and tracker handles (declared in include/yas.h), and the host pose
 // algebra shared by the library.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -516,6 +517,163 @@ YAS_API int yas_map_device_bytes(yas_map *m, size_t *out) {
                                m->voxel_bytes() + sizeof(MapHeader) + sizeof(PosePair);
     return YAS_OK;
 }
+
+// ------------------------------------------------------------------ fusion
+// Grows the map to at least `want_slots` (power of two) slots and `want_blocks`
+// pool blocks; blocks keep their pool indices and contents, the table is
+// rebuilt.  The sticky error bits of earlier calls are kept.
+static int map_grow(yas_map *m, long long want_slots, long long want_blocks) {
+    YAS_TRY(read_header(m));
+    const unsigned n = std::min(m->hdr_host->n_alloc, (unsigned)m->cfg.max_blocks);
+    const unsigned old_bits = m->hdr_host->err_bits;
+    long long ns = m->cfg.hash_slots;
+    while (ns < want_slots) ns <<= 1;
+    const long long nb = std::max<long long>(m->cfg.max_blocks, want_blocks);
+    if (ns == m->cfg.hash_slots && nb == m->cfg.max_blocks) return YAS_OK;
+    if (ns > (1LL << 30) || nb > (1LL << 30)) return YAS_ERR_CAPACITY;
+    const size_t vb = m->cfg.voxel_format == YAS_VOXEL_F32 ? 8 : 4;
+    HashSlot *slots = nullptr;
+    unsigned long long *keys = nullptr;
+    void *voxels = nullptr;
+    int *visible = nullptr;
+    if (cudaMalloc(&slots, (size_t)ns * sizeof(HashSlot)) != cudaSuccess ||
+        cudaMalloc(&keys, (size_t)nb * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&voxels, (size_t)nb * kBlockVoxels * vb) != cudaSuccess ||
+        cudaMalloc(&visible, (size_t)nb * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(slots);
+        cudaFree(keys);
+        cudaFree(voxels);
+        cudaFree(visible);
+        return YAS_ERR_OOM;
+    }
+    YAS_TRY_CUDA(cudaMemsetAsync(slots, 0xff, (size_t)ns * sizeof(HashSlot), m->stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(keys, m->block_keys, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                 m->stream));
+    YAS_TRY_CUDA(cudaMemcpyAsync(voxels, m->voxels, (size_t)n * kBlockVoxels * vb, cudaMemcpyDeviceToDevice, m->stream));
+    YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->n_visible, 0, sizeof(unsigned), m->stream));
+    YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->err_bits, 0, sizeof(unsigned), m->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    cudaFree(m->slots);
+    cudaFree(m->block_keys);
+    cudaFree(m->voxels);
+    cudaFree(m->visible);
+    m->slots = slots;
+    m->block_keys = keys;
+    m->voxels = voxels;
+    m->visible = visible;
+    m->cfg.hash_slots = (int)ns;
+    m->cfg.max_blocks = (int)nb;
+    m->slot_mask = (unsigned)(ns - 1);
+    launch_rehash(map_view(m), n, m->stream);
+    YAS_TRY_CUDA(cudaGetLastError());
+    YAS_TRY(read_header(m));
+    const bool full = (m->hdr_host->err_bits & err_bit(YAS_ERR_TABLE_FULL)) != 0;
+    const unsigned bits = old_bits | m->hdr_host->err_bits;
+    YAS_TRY_CUDA(cudaMemcpyAsync(&m->hdr->err_bits, &bits, sizeof(unsigned), cudaMemcpyHostToDevice, m->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    return full ? YAS_ERR_TABLE_FULL : YAS_OK;
+}
+
+extern "C" {
+
+YAS_API int yas_map_reserve(yas_map *m, int hash_slots, int max_blocks) {
+    if (!m || hash_slots <= 0 || max_blocks <= 0) return YAS_ERR_BAD_ARG;
+    if (m->hibernated) return YAS_ERR_STATE;
+    return map_grow(m, hash_slots, max_blocks);
+}
+
+YAS_API int yas_map_fuse_map(yas_map *dst, yas_map *src) {
+    if (!dst || !src || dst == src) return YAS_ERR_BAD_ARG;
+    if (dst->hibernated || src->hibernated) return YAS_ERR_STATE;
+    if (dst->cfg.voxel_format != src->cfg.voxel_format || dst->cfg.voxel_size != src->cfg.voxel_size)
+        return YAS_ERR_BAD_ARG;
+    YAS_TRY(read_header(src));
+    YAS_TRY(read_header(dst));
+    const unsigned nsrc = std::min(src->hdr_host->n_alloc, (unsigned)src->cfg.max_blocks);
+    const unsigned ndst = std::min(dst->hdr_host->n_alloc, (unsigned)dst->cfg.max_blocks);
+    if (nsrc == 0) return YAS_OK;
+    if (ndst == 0) {
+        // Swap: the destination takes the source's storage, configuration and
+        // pose; the source is left with the empty storage.
+        std::swap(dst->cfg, src->cfg);
+        std::swap(dst->slots, src->slots);
+        std::swap(dst->slot_mask, src->slot_mask);
+        std::swap(dst->block_keys, src->block_keys);
+        std::swap(dst->voxels, src->voxels);
+        std::swap(dst->visible, src->visible);
+        std::swap(dst->hdr, src->hdr);
+        std::lock_guard<std::mutex> a(dst->pose_mutex), b(src->pose_mutex);
+        std::swap(dst->Tcw, src->Tcw);
+        return YAS_OK;
+    }
+    Pose64 Td, Ts;
+    {
+        std::lock_guard<std::mutex> a(dst->pose_mutex), b(src->pose_mutex);
+        Td = dst->Tcw;
+        Ts = src->Tcw;
+    }
+    const Rigid32 T_src_dst = rigid_from(pose_mul(pose_inverse(Td), Ts));
+    const Rigid32 T_dst_src = rigid_from(pose_mul(pose_inverse(Ts), Td));
+    // room for the source's blocks in the destination (the reference reserves
+    // both maps' capacities), grown again if they spread over more blocks
+    long long want_blocks = (long long)ndst + 2LL * nsrc;
+    YAS_TRY(map_grow(dst, 2 * want_blocks, want_blocks));
+    YAS_TRY_CUDA(cudaMemsetAsync(&dst->hdr->err_bits, 0, sizeof(unsigned), dst->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(src->stream));
+    for (int attempt = 0;; ++attempt) {
+        launch_fuse_alloc(map_view(dst), map_view(src), dst->cfg.voxel_format, T_src_dst, nsrc, dst->stream);
+        YAS_TRY_CUDA(cudaGetLastError());
+        YAS_TRY(read_header(dst));
+        const unsigned e = dst->hdr_host->err_bits;
+        if (e & err_bit(YAS_ERR_COORD_RANGE)) return YAS_ERR_COORD_RANGE;
+        if (!(e & (err_bit(YAS_ERR_POOL_FULL) | err_bit(YAS_ERR_TABLE_FULL)))) break;
+        if (attempt == 3) return (e & err_bit(YAS_ERR_POOL_FULL)) ? YAS_ERR_POOL_FULL : YAS_ERR_TABLE_FULL;
+        // keys claimed without a pool block are dropped by the rebuild; the
+        // next pass inserts them again
+        if (dst->hdr_host->n_alloc > (unsigned)dst->cfg.max_blocks) {
+            const unsigned cap = (unsigned)dst->cfg.max_blocks;
+            YAS_TRY_CUDA(cudaMemcpyAsync(&dst->hdr->n_alloc, &cap, sizeof(unsigned), cudaMemcpyHostToDevice,
+                                         dst->stream));
+        }
+        YAS_TRY_CUDA(cudaMemsetAsync(&dst->hdr->err_bits, 0, sizeof(unsigned), dst->stream));
+        want_blocks *= 2;
+        YAS_TRY(map_grow(dst, 2 * want_blocks, want_blocks));
+    }
+    launch_fuse_blend(map_view(dst), map_view(src), dst->cfg.voxel_format, T_dst_src, dst->stream);
+    YAS_TRY_CUDA(cudaGetLastError());
+    YAS_TRY_CUDA(cudaStreamSynchronize(dst->stream));
+    // the reference releases the source's storage; here it is emptied and its
+    // handle stays valid until yas_map_destroy
+    return yas_map_reset(src);
+}
+
+YAS_API int yas_map_defuse_depth(yas_map *m, const float *depth, int width, int height, int pitch_bytes,
+                                 int on_device, const yas_pose *Tcm) {
+    if (!m || !depth || !Tcm || width <= 0 || height <= 0 || pitch_bytes < width * 4 || (pitch_bytes & 3))
+        return YAS_ERR_BAD_ARG;
+    if (m->hibernated) return YAS_ERR_STATE;
+    const float *d = depth;
+    if (!on_device) {
+        MapExtra *ex = map_extra(m);
+        YAS_TRY(ex->depth.ensure((size_t)pitch_bytes * height));
+        YAS_TRY_CUDA(cudaMemcpyAsync(ex->depth.ptr, depth, (size_t)pitch_bytes * height, cudaMemcpyHostToDevice,
+                                     m->stream));
+        d = (const float *)ex->depth.ptr;
+    }
+    PosePair pp = make_pair(Tcm);
+    YAS_TRY_CUDA(cudaMemcpyAsync(m->pose_dev, &pp, sizeof(pp), cudaMemcpyHostToDevice, m->stream));
+    Cam cam = make_cam(m->cam_K.fx, m->cam_K.fy, m->cam_K.cx, m->cam_K.cy, width, height);
+    MapDev v = map_view(m);
+    YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->n_visible, 0, sizeof(unsigned), m->stream));
+    launch_visible(v, cam, m->pose_dev, nullptr, m->stream);
+    launch_deintegrate(v, m->cfg.voxel_format, d, pitch_bytes / 4, cam, m->pose_dev, m->stream);
+    YAS_TRY_CUDA(cudaGetLastError());
+    if (!on_device) YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    return YAS_OK;
+}
+
+}  // extern "C"
 
 // ------------------------------------------------------------------ raycaster
 YAS_API int yas_raycaster_create(yas_raycaster **out, int width, int height, const yas_intrinsics *K, void *stream) {

@@ -90,7 +90,6 @@ __global__ void __launch_bounds__(256) allocate_kernel(MapDev m, const float *__
     if (skip && *skip) return;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    const unsigned lane = lane_id();
     const Rigid32 T = P->T;
 
     BlockLine line;
@@ -127,42 +126,7 @@ __global__ void __launch_bounds__(256) allocate_kernel(MapDev m, const float *__
                 has = false;
             }
         }
-        // Warp-level de-duplication: one leader per distinct key.
-        unsigned peers = __match_any_sync(0xffffffffu, key);
-        bool leader = has && (__ffs(peers) - 1) == (int)lane;
-        int claimed = 0;
-        unsigned slot = 0;
-        if (leader) {
-            claimed = claim_slot(m, key, &slot);
-            if (claimed < 0) {
-                raise_error(m, YAS_ERR_TABLE_FULL);
-                claimed = 0;
-            }
-        }
-        // Warp-aggregated pool allocation: one atomicAdd per warp.
-        unsigned idx = warp_append(&m.hdr->n_alloc, claimed == 1);
-        bool ok = false;
-        if (claimed == 1) {
-            if (idx < (unsigned)m.max_blocks) {
-                m.block_keys[idx] = key;
-                m.slots[slot].ptr = (int)idx;
-                ok = true;
-            } else {
-                raise_error(m, YAS_ERR_POOL_FULL);
-            }
-        }
-        // Zero the new blocks with the whole warp (coalesced 16-byte stores).
-        unsigned newmask = __ballot_sync(0xffffffffu, ok);
-        while (newmask) {
-            int src = __ffs(newmask) - 1;
-            newmask &= newmask - 1;
-            unsigned b = __shfl_sync(0xffffffffu, idx, src);
-            uint4 *dst = reinterpret_cast<uint4 *>(static_cast<char *>(m.voxels) +
-                                                   (size_t)b * kBlockVoxels * VBYTES);
-            constexpr int n16 = kBlockVoxels * VBYTES / 16;
-#pragma unroll
-            for (int i = lane; i < n16; i += 32) dst[i] = make_uint4(0, 0, 0, 0);
-        }
+        warp_insert<VBYTES>(m, key, has);
     }
 }
 
@@ -236,7 +200,11 @@ __device__ __forceinline__ int project_exact(float a, float z, float rz, float c
 
 // Each 128-thread group owns one block; thread t updates voxels 4t..4t+3
 // (z = t/16, y = (t/2)%8, x = 4*(t%2) .. +3), one 16-byte (or 32-byte) access.
-template <int FMT>
+// SIGN = +1: DepthFusionFunctor (VoxelMap.cu:719-786).  SIGN = -1: the same
+// observation removed again (de-integration, for re-integration after a pose
+// correction): s <- (s w - d) / (w - 1), w <- w - 1; exact while the weight
+// stayed below the cap, as the reference's running average is then invertible.
+template <int FMT, int SIGN>
 __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *__restrict__ depth,
                                                         int pitch, Cam cam, const PosePair *P,
                                                         const int *skip) {
@@ -287,12 +255,23 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
             sdf = fminf(1.0f, sdf * inv_trunc);
             int w = IO::wt(v[q]);
             float ns;
-            if (w == 0) {
-                ns = sdf;
-                w = 1;
+            if (SIGN > 0) {
+                if (w == 0) {
+                    ns = sdf;
+                    w = 1;
+                } else {
+                    ns = __fdividef(fmaf(IO::sdf(v[q]), (float)w, sdf), (float)(w + 1));
+                    w = min(m.max_weight, w + 1);
+                }
             } else {
-                ns = __fdividef(fmaf(IO::sdf(v[q]), (float)w, sdf), (float)(w + 1));
-                w = min(m.max_weight, w + 1);
+                if (w == 0) continue;
+                if (w == 1) {
+                    ns = 0.0f;
+                    w = 0;
+                } else {
+                    ns = __fdividef(fmaf(IO::sdf(v[q]), (float)w, -sdf), (float)(w - 1));
+                    w = w - 1;
+                }
             }
             v[q] = IO::make(ns, w);
             dirty = true;
@@ -318,20 +297,31 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
     }
 }
 
-void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                      const PosePair *P, const int *skip, cudaStream_t s) {
+template <int SIGN>
+static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
+                                  const PosePair *P, const int *skip, cudaStream_t s) {
     const int grid = 152 * 8;
     switch (fmt) {
         case YAS_VOXEL_F32:
-            integrate_kernel<YAS_VOXEL_F32><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            integrate_kernel<YAS_VOXEL_F32, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
             break;
         case YAS_VOXEL_F16:
-            integrate_kernel<YAS_VOXEL_F16><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            integrate_kernel<YAS_VOXEL_F16, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
             break;
         default:
-            integrate_kernel<YAS_VOXEL_S24><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            integrate_kernel<YAS_VOXEL_S24, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
             break;
     }
+}
+
+void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
+                      const PosePair *P, const int *skip, cudaStream_t s) {
+    launch_integrate_sign<1>(m, fmt, depth, pitch_elems, cam, P, skip, s);
+}
+
+void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
+                        const PosePair *P, cudaStream_t s) {
+    launch_integrate_sign<-1>(m, fmt, depth, pitch_elems, cam, P, nullptr, s);
 }
 
 // ---------------------------------------------------------------- reset

@@ -240,4 +240,47 @@ __device__ __forceinline__ unsigned warp_append(unsigned *counter, bool pred) {
     return pred ? base + (unsigned)__popc(mask & lanemask_lt()) : 0xffffffffu;
 }
 
+// Warp-cooperative insertion of one block key per lane (lanes with !has
+// insert nothing; all 32 lanes call together): duplicates within the warp
+// merge into one leader, each new key claims a hash slot (CAS), takes the
+// next pool block (one atomicAdd per warp) and the warp zeroes the new blocks
+// with coalesced 16-byte stores.  Table and pool exhaustion set the map's
+// sticky error bits (CreateNewBlock, VoxelStructUtils.h:259-280).
+template <int VBYTES>
+__device__ __forceinline__ void warp_insert(const MapDev &m, unsigned long long key, bool has) {
+    const unsigned lane = lane_id();
+    const unsigned peers = __match_any_sync(0xffffffffu, has ? key : kEmptyKey);
+    const bool leader = has && (__ffs(peers) - 1) == (int)lane;
+    int claimed = 0;
+    unsigned slot = 0;
+    if (leader) {
+        claimed = claim_slot(m, key, &slot);
+        if (claimed < 0) {
+            raise_error(m, YAS_ERR_TABLE_FULL);
+            claimed = 0;
+        }
+    }
+    const unsigned idx = warp_append(&m.hdr->n_alloc, claimed == 1);
+    bool ok = false;
+    if (claimed == 1) {
+        if (idx < (unsigned)m.max_blocks) {
+            m.block_keys[idx] = key;
+            m.slots[slot].ptr = (int)idx;
+            ok = true;
+        } else {
+            raise_error(m, YAS_ERR_POOL_FULL);
+        }
+    }
+    unsigned newmask = __ballot_sync(0xffffffffu, ok);
+    while (newmask) {
+        const int src = __ffs(newmask) - 1;
+        newmask &= newmask - 1;
+        const unsigned b = __shfl_sync(0xffffffffu, idx, src);
+        uint4 *dst = reinterpret_cast<uint4 *>(static_cast<char *>(m.voxels) + (size_t)b * kBlockVoxels * VBYTES);
+        constexpr int n16 = kBlockVoxels * VBYTES / 16;
+#pragma unroll
+        for (int i = (int)lane; i < n16; i += 32) dst[i] = make_uint4(0, 0, 0, 0);
+    }
+}
+
 }  // namespace yas

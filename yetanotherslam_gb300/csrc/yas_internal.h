@@ -73,6 +73,13 @@ void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const in
 // Integrates depth into the visible blocks.
 void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
                       const PosePair *P, const int *skip, cudaStream_t s);
+void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
+                        const PosePair *P, cudaStream_t s);
+// Submap fusion and growth (fusion.cu)
+void launch_rehash(const MapDev &m, unsigned n, cudaStream_t s);
+void launch_fuse_alloc(const MapDev &dst, const MapDev &src, int fmt, const Rigid32 &T_src_dst, unsigned nsrc,
+                       cudaStream_t s);
+void launch_fuse_blend(const MapDev &dst, const MapDev &src, int fmt, const Rigid32 &T_dst_src, cudaStream_t s);
 void launch_map_reset(const MapDev &m, cudaStream_t s);
 void launch_map_export(const MapDev &m, int fmt, int *coords, float *sdf, float *wt, unsigned first,
                        unsigned count, cudaStream_t s);

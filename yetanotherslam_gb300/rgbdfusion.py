@@ -116,6 +116,20 @@ class MapStruct:
         h, w = depth.shape[:2]
         L.call("yas_map_fuse_depth", self.handle, ptr, w, h, pitch, dev, C.byref(L.pose_from(Tcm)))
 
+    # MapStruct::Fuse(MapStruct*): fuse another submap into this one (src is left empty)
+    def FuseMap(self, src: "MapStruct") -> None:
+        L.call("yas_map_fuse_map", self.handle, src.handle)
+
+    # MapStruct::Reserve(hashTableSize, bucketSize, voxelBlockSize)
+    def Reserve(self, hash_slots: int, max_blocks: int) -> None:
+        L.call("yas_map_reserve", self.handle, hash_slots, max_blocks)
+
+    def Defuse(self, depth, Tcm) -> None:
+        """Removes the observation of `depth` at Tcm (re-integration after a pose correction)."""
+        ptr, pitch, dev, keep = _device_info(depth)
+        h, w = depth.shape[:2]
+        L.call("yas_map_defuse_depth", self.handle, ptr, w, h, pitch, dev, C.byref(L.pose_from(Tcm)))
+
     def CheckNumVisibleBlocks(self, cols: int, rows: int, Tcm) -> int:
         out = C.c_uint()
         L.call("yas_map_check_visible", self.handle, cols, rows, C.byref(L.pose_from(Tcm)), C.byref(out))
