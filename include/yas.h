@@ -45,7 +45,8 @@ enum yas_status {
     YAS_ERR_STATE = 9,         /* call not valid in the handle's state       */
     YAS_ERR_COORD_RANGE = 10,  /* block coordinate outside the 21-bit range  */
     YAS_ERR_CAPACITY = 11,     /* caller buffer too small                    */
-    YAS_ERR_TIMEOUT = 12       /* a bounded device-side wait gave up         */
+    YAS_ERR_TIMEOUT = 12,      /* a bounded device-side wait gave up         */
+    YAS_ERR_IO = 13            /* a file could not be read or written        */
 };
 
 /* Human-readable name of a status code (static string). */
@@ -144,6 +145,15 @@ YAS_API int yas_map_device_bytes(yas_map *map, size_t *out_bytes);
  * grows the table to >= hash_slots slots (power of two) and the pool to
  * >= max_blocks blocks; blocks keep their contents, the table is rebuilt. */
 YAS_API int yas_map_reserve(yas_map *map, int hash_slots, int max_blocks);
+/* MapStruct::SaveToFile / ReadFromFile (VoxelMap.h:65-66; empty stubs at
+ * VoxelMap.cu:886-893): a binary submap file (144-byte header: magic
+ * "YASSUBM1", version 1, voxel format, voxel size, truncation, depth gates,
+ * weight cap, capacities, block count, pose; then int32 block coordinates; then
+ * the voxels in the map's storage format).  Loading replaces the map's
+ * contents and pose, grows it if needed, and needs the same voxel format and
+ * size (YAS_ERR_BAD_ARG otherwise); the round trip is bit-exact. */
+YAS_API int yas_map_save(yas_map *map, const char *path);
+YAS_API int yas_map_load(yas_map *map, const char *path);
 /* MapStruct::Fuse(MapStruct *src), VoxelMap.cu:398-444 (System::FuseAllMapStruct,
  * System.cpp:73-93): fuses src into map using both maps' poses (yas_map_get_pose);
  * an empty map takes src's storage and pose.  src is left empty (the reference
@@ -280,6 +290,15 @@ typedef struct yas_gn_level {
 YAS_API int yas_gn_linearise_static(const yas_gn_level *level, const yas_pose *T, int mode, double *dev_out,
                                     void *stream);
 
+/* ---------------------------------------------------------------- shading
+ * RenderScene(vmap, nmap, image), ImageProc.cu:128-139 (ImageProc.h:17): Phong
+ * shading of a device vertex/normal map (float4, camera frame, the same row
+ * pitch) into RGBA8 for display, headless (no GL).  light: 3 floats in the
+ * camera frame (NULL: the reference's (5, 5, 5)).  rgba: device memory
+ * (on_device = 1) or host memory (0, copied back before return). */
+YAS_API int yas_render_scene(const float *dev_vmap, const float *dev_nmap, int width, int height, int pitch_bytes,
+                             const float *light, uint8_t *rgba, int out_pitch_bytes, int on_device, void *stream);
+
 /* ---------------------------------------------------------------- session
  * One SLAM session: a submap, a raycaster and a tracker whose per-frame dense
  * work (Tracking::TrackRGBD + Tracking::StereoInitialization dense calls,
@@ -321,6 +340,12 @@ YAS_API int yas_session_map(yas_session *s, yas_map **out);
 YAS_API int yas_session_tracker(yas_session *s, yas_tracker **out);
 YAS_API int yas_session_raycaster(yas_session *s, yas_raycaster **out);
 YAS_API int yas_session_frame_count(yas_session *s, int *out);
+/* The submap switch of Tracking::CreateNewKeyFrame (Tracking.cpp:700-718):
+ * the current submap is deactivated and handed to the caller (who owns it:
+ * yas_map_fuse_map or yas_map_destroy); a new empty submap with the same
+ * configuration, posed at the current camera's world pose (previous submap
+ * pose * Tcm), continues the session, and Tcm restarts at the identity. */
+YAS_API int yas_session_new_submap(yas_session *s, yas_map **out_previous);
 /* Device pointer of the session's float depth (metres) of the last frame. */
 YAS_API int yas_session_depth(yas_session *s, const float **dev_depth, int *pitch_bytes);
 /* Number of kernels the last frame launched (graph nodes of kind kernel). */
@@ -378,6 +403,13 @@ YAS_API int yas_server_destroy(yas_server *srv);
 /* Admits a session (YAS_ERR_OOM: its footprint does not fit the free HBM minus
  * the reserve; YAS_ERR_CAPACITY: max_sessions live). */
 YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *cfg, int *out_id);
+/* Eviction (MapStruct::Hibernate / ReActivate, VoxelMap.cu:894-954): suspend
+ * waits for the session's frame in flight and moves its map to host memory,
+ * freeing its HBM; frames submitted meanwhile stay queued.  Resume is admitted
+ * like a new session (YAS_ERR_OOM if the map does not fit the free HBM minus
+ * the reserve) and brings the map back. */
+YAS_API int yas_server_suspend_session(yas_server *srv, int id);
+YAS_API int yas_server_resume_session(yas_server *srv, int id);
 /* Drops the session's queued frames, waits for its frame in flight, frees it. */
 YAS_API int yas_server_close_session(yas_server *srv, int id);
 /* Queues one frame (host RGB u8 interleaved, depth u16; copied before the call

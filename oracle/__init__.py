@@ -48,6 +48,7 @@ _SIGS = {
     "orc_session_tracker": ([_P], _P),
     "orc_map_defuse": ([_P, _P, _I, _I, _P, _P], _I),
     "orc_map_fuse_map": ([_P, _P, _P, _P], _I),
+    "orc_render_scene": ([_P, _P, _I, _I, _P, _P], None),
     "orc_se3_exp": ([_P, _P], None),
     "orc_ldlt_solve6": ([_P, _P, _P], None),
     "orc_real_bytes": ([], _I),
@@ -243,6 +244,17 @@ class Session:
             return m.export()
         finally:
             m.h = None
+
+
+def render_scene(vmap: np.ndarray, nmap: np.ndarray, light=(5.0, 5.0, 5.0)) -> np.ndarray:
+    """RenderScene: (h, w, 4) float vertex/normal maps -> (h, w, 4) uint8."""
+    v = np.ascontiguousarray(vmap, dtype=np.float32)
+    n = np.ascontiguousarray(nmap, dtype=np.float32)
+    h, w = v.shape[:2]
+    out = np.zeros((h, w, 4), np.uint8)
+    lt = np.asarray(light, dtype=np.float32)
+    lib().orc_render_scene(_ptr(v), _ptr(n), w, h, _ptr(lt), _ptr(out))
+    return out
 
 
 def se3_exp(xi) -> np.ndarray:

@@ -65,6 +65,8 @@ void orc_map_import(orc_map *m, const int *coords, const float *sdf, const float
 void orc_raycast(orc_map *m, int w, int h, const float *K, const double *Tcm, float *vmap, float *znear, float *zfar);
 /* Marching cubes over all blocks: tris 9 floats each, cases, cube_xyz; returns
  * the number of triangles (writes at most cap). */
+/* RenderScene: Phong shading of a vertex/normal map (float4, w*h) into RGBA8. */
+void orc_render_scene(const float *vmap, const float *nmap, int w, int h, const float *light, unsigned char *rgba);
 int orc_mesh(const orc_map *m, float *tris, float *normals, int *cases, int *cube_xyz, int cap);
 void orc_mc_tables(unsigned short *edge, signed char *tri, unsigned char *count);
 

@@ -815,3 +815,41 @@ int orc_mesh(const orc_map *m, float *tris, float *normals, int *cases, int *cub
 }
 
 int orc_real_bytes(void) { return (int)sizeof(real); }
+
+/* ------------------------------------------------------------ shading
+ * RenderScene (ImageProc.cu:80-139): Phong shading, white surface, ambient
+ * 0.3, diffuse 0.5, specular 0.2 with power 20, point light in the camera
+ * frame; a pixel without a vertex is (4, 2, 2, 255). */
+static void normalise3(float *v) {
+    const float n = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= n;
+    v[1] /= n;
+    v[2] /= n;
+}
+
+void orc_render_scene(const float *vmap, const float *nmap, int w, int h, const float *light, unsigned char *rgba) {
+    for (int i = 0; i < w * h; ++i) {
+        const float *p = vmap + 4 * (size_t)i, *nr = nmap + 4 * (size_t)i;
+        unsigned char *o = rgba + 4 * (size_t)i;
+        if (isnan(p[0])) {
+            o[0] = 4;
+            o[1] = 2;
+            o[2] = 2;
+            o[3] = 255;
+            continue;
+        }
+        float L[3] = {light[0] - p[0], light[1] - p[1], light[2] - p[2]};
+        float V[3] = {-p[0], -p[1], -p[2]};
+        normalise3(L);
+        normalise3(V);
+        const float nl = nr[0] * L[0] + nr[1] * L[1] + nr[2] * L[2];
+        float R[3] = {2.0f * nr[0] * nl - L[0], 2.0f * nr[1] * nl - L[1], 2.0f * nr[2] * nl - L[2]};
+        normalise3(R);
+        const float rv = R[0] * V[0] + R[1] * V[1] + R[2] * V[2];
+        float I = 0.3f + 0.5f * fmaxf(0.0f, nl) + 0.2f * powf(fmaxf(0.0f, rv), 20.0f);
+        I = I < 0.0f ? 0.0f : (I > 1.0f ? 1.0f : I);
+        const unsigned char c = (unsigned char)(I * 255.0f);
+        o[0] = o[1] = o[2] = c;
+        o[3] = 255;
+    }
+}

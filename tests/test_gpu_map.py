@@ -15,6 +15,7 @@ import pytest
 
 import oracle
 from tests.helpers import align_blocks, rel_poses, sequence
+from yetanotherslam_gb300 import _lib as L
 from yetanotherslam_gb300 import rgbdfusion as rf
 from yetanotherslam_gb300 import synth
 
@@ -191,3 +192,42 @@ def test_reset_clears_map(cuda):
     o = oracle.Map(0.008, 0.024)
     o.fuse(dm, K, np.eye(4))
     assert m.num_allocated() == o.num_blocks
+
+
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16])
+def test_submap_file_roundtrip(cuda, fmt, tmp_path):
+    """SaveToFile / ReadFromFile: the round trip is bit-exact, the loaded map
+    (grown from a small capacity) fuses on exactly as the original, a format
+    mismatch is refused and a missing file reports YAS_ERR_IO."""
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, 4, W, H)
+    poses = rel_poses(seq)
+    a, _ = _pair(fmt, K)
+    for i in range(3):
+        a.Fuse(seq[i][2], poses[i])
+    T = np.eye(4)
+    T[:3, 3] = [0.1, -0.2, 0.3]
+    a.SetPose(T)
+    path = tmp_path / "submap.yas"
+    a.SaveToFile(path)
+    b = rf.MapStruct(K)
+    b.create_config(1 << 10, 64, 0.008, 0.024, fmt)
+    b.ReadFromFile(path)
+    for x, y in zip(a.export(), b.export()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(b.GetPose(), a.GetPose())
+    a.Fuse(seq[3][2], poses[3])
+    b.Fuse(seq[3][2], poses[3])
+    ca, sa, wa = a.export()
+    cb, sb, wb = b.export()
+    sa, wa, sb, wb = align_blocks(ca, sa, wa, cb, sb, wb)
+    assert np.array_equal(sa, sb) and np.array_equal(wa, wb)
+    other = rf.MapStruct(K)
+    other.create_config(1 << 14, 1 << 12, 0.008, 0.024, rf.VOXEL_S24)
+    with pytest.raises(L.YasError) as e:
+        other.ReadFromFile(path)
+    assert e.value.code == 1
+    with pytest.raises(L.YasError) as e:
+        b.ReadFromFile(tmp_path / "missing.yas")
+    assert e.value.code == 13

@@ -97,3 +97,32 @@ def test_admission_by_free_hbm(cuda):
         srv.open(320, 240, synth.intrinsics(320, 240), **MAP)
     assert e.value.code == 2  # YAS_ERR_OOM: not admitted
     srv.close()
+
+
+def test_suspend_and_resume_session(cuda):
+    """A suspended session's map leaves HBM; frames submitted meanwhile wait
+    and, after resume, give the poses of an uninterrupted run."""
+    import torch
+
+    W, H, n = 320, 240, 6
+    seq = sequence(3, n, W, H)
+    alone = _serve_alone(seq, W, H)
+    srv = serving.Server(hbm_reserve_bytes=1 << 30)
+    sid = srv.open(W, H, synth.intrinsics(W, H), **MAP)
+    for rgb, d16, _, _ in seq[:3]:
+        assert srv.submit(sid, rgb, d16) == 0
+        srv.drain()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    srv.suspend(sid)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 - free0 >= (MAP["max_blocks"] * 512 * 4) // 2  # the voxel pool was released
+    for rgb, d16, _, _ in seq[3:]:
+        assert srv.submit(sid, rgb, d16) == 0
+    srv.resume(sid)
+    srv.drain()
+    res = sorted(srv.poll(64), key=lambda r: r["frame"])
+    srv.close()
+    assert [r["frame"] for r in res] == list(range(n))
+    for r, T in zip(res, alone):
+        assert r["status"] == 0 and np.array_equal(r["Tcm"], T)

@@ -113,3 +113,53 @@ def test_lost_frame_is_rejected_and_map_unchanged(cuda):
         assert np.array_equal(c1, c2) and np.array_equal(x1, x2) and np.array_equal(w1, w2)
     else:
         assert st == 0
+
+
+def test_submap_switch_keeps_tracking(cuda):
+    """CreateNewKeyFrame's submap switch (Tracking.cpp:700-718): the previous
+    submap is handed over inactive and non-empty; the new one starts at the
+    camera's world pose and tracking continues, so the world trajectory
+    (submap pose * Tcm) stays on the ground truth within the session bars."""
+    W, H, n, k = 320, 240, 12, 6
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, n, W, H)
+    gt = rel_poses(seq)
+    s = rf.Session(W, H, K, hash_slots=1 << 20, max_blocks=1 << 17, voxel_size=0.008)
+    world = []
+    prev = None
+    for i, (rgb, d16, _, _) in enumerate(seq):
+        if i == k:
+            prev = s.new_submap()
+        st, T = s.process(rgb, d16)
+        assert st == 0
+        world.append(s.map().GetPose() @ T)
+    assert prev is not None and not prev.isActive() and not prev.Empty()
+    assert np.allclose(prev.GetPose(), np.eye(4))
+    assert np.allclose(s.map().GetPose(), world[k - 1], atol=1e-9)
+    assert not s.map().Empty()
+    for i in range(n):
+        et, er = pose_error(gt[i], world[i])
+        assert et < 0.05 and er < 0.02, (i, et, er)
+    prev.Release()
+
+
+def test_hibernate_mid_sequence_recaptures_frames(cuda):
+    """Hibernating and reactivating the session's map moves its device arrays;
+    the session captures its frame graphs again, so the poses equal an
+    uninterrupted run bit for bit, and a hibernated map refuses frames."""
+    from yetanotherslam_gb300 import _lib as L
+
+    W, H, n = 160, 120, 8
+    _, ref = _run(W, H, n, rf.VOXEL_F16, True)
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, n, W, H)
+    s = rf.Session(W, H, K, hash_slots=1 << 20, max_blocks=1 << 17, voxel_size=0.008, voxel_format=rf.VOXEL_F16)
+    for i, (rgb, d16, _, _) in enumerate(seq):
+        if i == n // 2:
+            s.map().Hibernate()
+            with pytest.raises(L.YasError) as e:
+                s.process(rgb, d16)
+            assert e.value.code == 9  # YAS_ERR_STATE
+            s.map().ReActivate()
+        st, T = s.process(rgb, d16)
+        assert st == 0 and np.array_equal(T, ref[i]), i

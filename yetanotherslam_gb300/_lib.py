@@ -20,6 +20,7 @@ STATUS = {
     0: "YAS_OK", 1: "YAS_ERR_BAD_ARG", 2: "YAS_ERR_OOM", 3: "YAS_ERR_CUDA", 4: "YAS_ERR_TABLE_FULL",
     5: "YAS_ERR_POOL_FULL", 6: "YAS_ERR_NUMERIC", 7: "YAS_ERR_TRACK_LOST", 8: "YAS_ERR_MESH_OVERFLOW",
     9: "YAS_ERR_STATE", 10: "YAS_ERR_COORD_RANGE", 11: "YAS_ERR_CAPACITY", 12: "YAS_ERR_TIMEOUT",
+    13: "YAS_ERR_IO",
 }
 VOXEL_F32, VOXEL_F16, VOXEL_S24 = 0, 1, 2
 TRACK_RGB, TRACK_ICP, TRACK_RGBD = 1, 2, 3
@@ -107,6 +108,8 @@ _SIGS = {
     "yas_map_is_hibernated": [_P, _PI],
     "yas_map_device_bytes": [_P, C.POINTER(C.c_size_t)],
     "yas_map_reserve": [_P, _I, _I],
+    "yas_map_save": [_P, C.c_char_p],
+    "yas_map_load": [_P, C.c_char_p],
     "yas_map_fuse_map": [_P, _P],
     "yas_map_defuse_depth": [_P, _P, _I, _I, _I, _I, C.POINTER(Pose)],
     "yas_raycaster_create": [_PP, _I, _I, C.POINTER(Intrinsics), _P],
@@ -146,17 +149,21 @@ _SIGS = {
     "yas_session_tracker": [_P, _PP],
     "yas_session_raycaster": [_P, _PP],
     "yas_session_frame_count": [_P, _PI],
+    "yas_session_new_submap": [_P, _PP],
     "yas_session_depth": [_P, _PP, _PI],
     "yas_session_kernels_per_frame": [_P, _PI],
     "yas_session_stream": [_P],
     "yas_session_profile_frame": [_P, _P, _P, _I, _P, _P, _I, _PI],
     "yas_mc_tables": [_P, _P, _P],
+    "yas_render_scene": [_P, _P, _I, _I, _I, _P, _P, _I, _I, _P],
     "yas_gn_linearise_static": [C.POINTER(GnLevel), C.POINTER(Pose), _I, _P, _P],
     "yas_server_config_default": [C.POINTER(ServerConfig)],
     "yas_server_create": [_PP, C.POINTER(ServerConfig)],
     "yas_server_destroy": [_P],
     "yas_server_open_session": [_P, C.POINTER(SessionConfig), _PI],
     "yas_server_close_session": [_P, _I],
+    "yas_server_suspend_session": [_P, _I],
+    "yas_server_resume_session": [_P, _I],
     "yas_server_submit": [_P, _I, _P, _P],
     "yas_server_poll": [_P, C.POINTER(ServedResult), _I, _PI],
     "yas_server_drain": [_P, C.c_double],

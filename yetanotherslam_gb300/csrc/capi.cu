@@ -152,6 +152,7 @@ YAS_API const char *yas_status_string(int s) {
         case YAS_ERR_COORD_RANGE: return "block coordinate outside the key range";
         case YAS_ERR_CAPACITY: return "caller buffer too small";
         case YAS_ERR_TIMEOUT: return "device-side wait timed out";
+        case YAS_ERR_IO: return "file could not be read or written";
         default: return "unknown status";
     }
 }
@@ -466,7 +467,13 @@ YAS_API int yas_map_hibernate(yas_map *m) {
     m->hib_slots.resize(nslots * sizeof(HashSlot));
     m->hib_keys.resize((size_t)n * 8);
     m->hib_voxels.resize((size_t)n * vb);
+    // the visible list of the last fusion (the next raycast starts from it)
+    const unsigned nv = std::min(m->hib_hdr.n_visible, (unsigned)m->cfg.max_blocks);
+    m->hib_visible.resize((size_t)nv * sizeof(int));
     YAS_TRY_CUDA(cudaMemcpyAsync(m->hib_slots.data(), m->slots, m->hib_slots.size(), cudaMemcpyDeviceToHost, m->stream));
+    if (nv)
+        YAS_TRY_CUDA(cudaMemcpyAsync(m->hib_visible.data(), m->visible, m->hib_visible.size(), cudaMemcpyDeviceToHost,
+                                     m->stream));
     if (n) {
         YAS_TRY_CUDA(cudaMemcpyAsync(m->hib_keys.data(), m->block_keys, m->hib_keys.size(), cudaMemcpyDeviceToHost,
                                      m->stream));
@@ -491,9 +498,14 @@ YAS_API int yas_map_reactivate(yas_map *m) {
                                      m->stream));
     }
     MapHeader h = m->hib_hdr;
-    h.n_visible = 0;
+    h.n_visible = (unsigned)(m->hib_visible.size() / sizeof(int));
+    if (h.n_visible)
+        YAS_TRY_CUDA(cudaMemcpyAsync(m->visible, m->hib_visible.data(), m->hib_visible.size(), cudaMemcpyHostToDevice,
+                                     m->stream));
     YAS_TRY_CUDA(cudaMemcpyAsync(m->hdr, &h, sizeof(h), cudaMemcpyHostToDevice, m->stream));
     YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    m->hib_visible.clear();
+    m->hib_visible.shrink_to_fit();
     m->hib_slots.clear();
     m->hib_slots.shrink_to_fit();
     m->hib_keys.clear();
@@ -517,6 +529,145 @@ YAS_API int yas_map_device_bytes(yas_map *m, size_t *out) {
                                m->voxel_bytes() + sizeof(MapHeader) + sizeof(PosePair);
     return YAS_OK;
 }
+
+// ------------------------------------------------------------------ submap file
+static int map_grow(yas_map *m, long long want_slots, long long want_blocks);
+
+// Binary submap file (little-endian): SubmapFileHeader, then n_blocks block
+// coordinates (int32 x, y, z), then n_blocks * 512 voxels in the map's own
+// storage format (8 bytes for F32, 4 for F16 and S24), pool order.
+struct SubmapFileHeader {
+    char magic[8];          // "YASSUBM1"
+    uint32_t version;       // 1
+    uint32_t voxel_format;  // enum yas_voxel_format
+    float voxel_size, trunc_dist, depth_min, depth_max;
+    int32_t max_weight, hash_slots, max_blocks;
+    uint32_t n_blocks;
+    double pose[12];        // map pose (Tcw), row-major [R | t]
+};
+static_assert(sizeof(SubmapFileHeader) == 144, "submap file header layout");
+static const char kSubmapMagic[8] = {'Y', 'A', 'S', 'S', 'U', 'B', 'M', '1'};
+
+extern "C" {
+
+YAS_API int yas_map_save(yas_map *m, const char *path) {
+    if (!m || !path) return YAS_ERR_BAD_ARG;
+    if (m->hibernated) return YAS_ERR_STATE;
+    YAS_TRY(read_header(m));
+    const unsigned n = std::min(m->hdr_host->n_alloc, (unsigned)m->cfg.max_blocks);
+    const size_t vb = (size_t)kBlockVoxels * (m->cfg.voxel_format == YAS_VOXEL_F32 ? 8 : 4);
+    std::vector<unsigned long long> keys(n);
+    std::vector<unsigned char> vox((size_t)n * vb);
+    if (n) {
+        YAS_TRY_CUDA(cudaMemcpyAsync(keys.data(), m->block_keys, (size_t)n * 8, cudaMemcpyDeviceToHost, m->stream));
+        YAS_TRY_CUDA(cudaMemcpyAsync(vox.data(), m->voxels, vox.size(), cudaMemcpyDeviceToHost, m->stream));
+        YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    }
+    SubmapFileHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kSubmapMagic, 8);
+    h.version = 1;
+    h.voxel_format = (uint32_t)m->cfg.voxel_format;
+    h.voxel_size = m->cfg.voxel_size;
+    h.trunc_dist = m->cfg.trunc_dist;
+    h.depth_min = m->cfg.depth_min;
+    h.depth_max = m->cfg.depth_max;
+    h.max_weight = m->cfg.max_weight;
+    h.hash_slots = m->cfg.hash_slots;
+    h.max_blocks = m->cfg.max_blocks;
+    h.n_blocks = n;
+    {
+        std::lock_guard<std::mutex> lk(m->pose_mutex);
+        const yas_pose p = pose_to(m->Tcw);
+        memcpy(h.pose, p.m, sizeof(h.pose));
+    }
+    std::vector<int32_t> coords((size_t)n * 3);
+    for (unsigned i = 0; i < n; ++i) unpack_key(keys[i], coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]);
+    FILE *f = fopen(path, "wb");
+    if (!f) return YAS_ERR_IO;
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    if (ok && n) ok = fwrite(coords.data(), sizeof(int32_t), coords.size(), f) == coords.size();
+    if (ok && n) ok = fwrite(vox.data(), 1, vox.size(), f) == vox.size();
+    ok = (fclose(f) == 0) && ok;
+    return ok ? YAS_OK : YAS_ERR_IO;
+}
+
+YAS_API int yas_map_load(yas_map *m, const char *path) {
+    if (!m || !path) return YAS_ERR_BAD_ARG;
+    if (m->hibernated) return YAS_ERR_STATE;
+    FILE *f = fopen(path, "rb");
+    if (!f) return YAS_ERR_IO;
+    SubmapFileHeader h;
+    bool ok = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, kSubmapMagic, 8) == 0 && h.version == 1;
+    const size_t vb = (size_t)kBlockVoxels * (h.voxel_format == YAS_VOXEL_F32 ? 8 : 4);
+    std::vector<int32_t> coords;
+    std::vector<unsigned char> vox;
+    if (ok) {
+        coords.resize((size_t)h.n_blocks * 3);
+        vox.resize((size_t)h.n_blocks * vb);
+        if (h.n_blocks)
+            ok = fread(coords.data(), sizeof(int32_t), coords.size(), f) == coords.size() &&
+                 fread(vox.data(), 1, vox.size(), f) == vox.size();
+    }
+    fclose(f);
+    if (!ok) return YAS_ERR_IO;
+    if ((int)h.voxel_format != m->cfg.voxel_format || h.voxel_size != m->cfg.voxel_size) return YAS_ERR_BAD_ARG;
+    const unsigned n = h.n_blocks;
+    std::vector<unsigned long long> keys(n);
+    for (unsigned i = 0; i < n; ++i) {
+        if (!coord_in_range(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2])) return YAS_ERR_COORD_RANGE;
+        keys[i] = pack_key(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]);
+    }
+    YAS_TRY(yas_map_reset(m));
+    YAS_TRY(map_grow(m, std::max<long long>(h.hash_slots, 2LL * n), std::max<long long>(h.max_blocks, n)));
+    if (n) {
+        YAS_TRY_CUDA(cudaMemcpyAsync(m->block_keys, keys.data(), (size_t)n * 8, cudaMemcpyHostToDevice, m->stream));
+        YAS_TRY_CUDA(cudaMemcpyAsync(m->voxels, vox.data(), vox.size(), cudaMemcpyHostToDevice, m->stream));
+        YAS_TRY_CUDA(cudaMemcpyAsync(&m->hdr->n_alloc, &n, sizeof(unsigned), cudaMemcpyHostToDevice, m->stream));
+        launch_rehash(map_view(m), n, m->stream);
+        YAS_TRY_CUDA(cudaGetLastError());
+    }
+    YAS_TRY(read_header(m));
+    if (m->hdr_host->err_bits & err_bit(YAS_ERR_TABLE_FULL)) return YAS_ERR_TABLE_FULL;
+    yas_pose p;
+    memcpy(p.m, h.pose, sizeof(p.m));
+    std::lock_guard<std::mutex> lk(m->pose_mutex);
+    m->Tcw = pose_from(p);
+    return YAS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ shading
+extern "C" {
+
+YAS_API int yas_render_scene(const float *dev_vmap, const float *dev_nmap, int width, int height, int pitch_bytes,
+                             const float *light, uint8_t *rgba, int out_pitch_bytes, int on_device, void *stream) {
+    if (!dev_vmap || !dev_nmap || !rgba || width <= 0 || height <= 0 || pitch_bytes < width * 16 ||
+        (pitch_bytes & 15) || out_pitch_bytes < width * 4 || (out_pitch_bytes & 3))
+        return YAS_ERR_BAD_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const float3 L = light ? make_float3(light[0], light[1], light[2]) : make_float3(5.0f, 5.0f, 5.0f);
+    uchar4 *out = reinterpret_cast<uchar4 *>(rgba);
+    void *tmp = nullptr;
+    if (!on_device) {
+        YAS_TRY_CUDA(cudaMallocAsync(&tmp, (size_t)out_pitch_bytes * height, s));
+        out = static_cast<uchar4 *>(tmp);
+    }
+    launch_render_scene(reinterpret_cast<const float4 *>(dev_vmap), reinterpret_cast<const float4 *>(dev_nmap),
+                        pitch_bytes / 16, width, height, L, out, out_pitch_bytes / 4, s);
+    cudaError_t e = cudaGetLastError();
+    if (!on_device) {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(rgba, tmp, (size_t)out_pitch_bytes * height, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(tmp, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    YAS_TRY_CUDA(e);
+    return YAS_OK;
+}
+
+}  // extern "C"
 
 // ------------------------------------------------------------------ fusion
 // Grows the map to at least `want_slots` (power of two) slots and `want_blocks`
@@ -551,7 +702,10 @@ static int map_grow(yas_map *m, long long want_slots, long long want_blocks) {
     YAS_TRY_CUDA(cudaMemcpyAsync(keys, m->block_keys, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
                                  m->stream));
     YAS_TRY_CUDA(cudaMemcpyAsync(voxels, m->voxels, (size_t)n * kBlockVoxels * vb, cudaMemcpyDeviceToDevice, m->stream));
-    YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->n_visible, 0, sizeof(unsigned), m->stream));
+    // pool indices do not move, so the visible list stays valid as it is
+    const unsigned nv = std::min(m->hdr_host->n_visible, (unsigned)m->cfg.max_blocks);
+    if (nv)
+        YAS_TRY_CUDA(cudaMemcpyAsync(visible, m->visible, (size_t)nv * sizeof(int), cudaMemcpyDeviceToDevice, m->stream));
     YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->err_bits, 0, sizeof(unsigned), m->stream));
     YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
     cudaFree(m->slots);

@@ -236,4 +236,42 @@ void launch_model_level(const float4 *prev, int pw, int w, int h, float4 *vmap, 
     model_level_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(prev, pw, w, h, vmap, nmap);
 }
 
+// ---------------------------------------------------------------- shading
+// RenderScene (ImageProc.cu:80-139): Phong shading of a vertex/normal map for
+// display, white surface (ambient 0.3, diffuse 0.5, specular 0.2, power 20),
+// point light at `light` (camera frame); a pixel without a vertex is
+// (4, 2, 2, 255).  Colour bytes are the saturated intensity * 255 truncated.
+__device__ __forceinline__ float3 normalised(float3 v) {
+    const float n = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    return make_float3(v.x / n, v.y / n, v.z / n);
+}
+
+__global__ void render_scene_kernel(const float4 *__restrict__ vmap, const float4 *__restrict__ nmap, int vpitch,
+                                    int w, int h, float3 light, uchar4 *__restrict__ out, int opitch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float4 p4 = vmap[(size_t)y * vpitch + x];
+    const float4 n4 = nmap[(size_t)y * vpitch + x];
+    uchar4 o = make_uchar4(4, 2, 2, 255);
+    if (!isnan(p4.x)) {
+        const float3 p = make_float3(p4.x, p4.y, p4.z), nrm = make_float3(n4.x, n4.y, n4.z);
+        const float3 L = normalised(make_float3(light.x - p.x, light.y - p.y, light.z - p.z));
+        const float3 V = normalised(make_float3(-p.x, -p.y, -p.z));
+        const float nl = nrm.x * L.x + nrm.y * L.y + nrm.z * L.z;
+        const float3 R = normalised(make_float3(2.0f * nrm.x * nl - L.x, 2.0f * nrm.y * nl - L.y, 2.0f * nrm.z * nl - L.z));
+        const float rv = R.x * V.x + R.y * V.y + R.z * V.z;
+        const float I = 0.3f + 0.5f * fmaxf(0.0f, nl) + 0.2f * powf(fmaxf(0.0f, rv), 20.0f);
+        const unsigned char c = (unsigned char)(__saturatef(I) * 255.0f);
+        o = make_uchar4(c, c, c, 255);
+    }
+    out[(size_t)y * opitch + x] = o;
+}
+
+void launch_render_scene(const float4 *vmap, const float4 *nmap, int vpitch, int w, int h, float3 light,
+                         uchar4 *out, int opitch, cudaStream_t s) {
+    dim3 block(32, 8);
+    dim3 grid((w + 31) / 32, (h + 7) / 8);
+    render_scene_kernel<<<grid, block, 0, s>>>(vmap, nmap, vpitch, w, h, light, out, opitch);
+}
+
 }  // namespace yas

@@ -64,6 +64,7 @@ struct ServedSession {
     cudaEvent_t ev_pre = nullptr, ev_done = nullptr;
     long long submitted = 0, completed = 0;
     bool closing = false;
+    bool suspended = false;  // map swapped out to host memory; frames wait in the queue
 };
 
 // Device footprint of a session with this configuration (map, pyramids,
@@ -220,7 +221,7 @@ void worker_main(yas_server *srv) {
         // every session with a queued frame and none in flight starts it now
         for (ServedSession *ss : srv->sessions) {
             if (!ss) continue;
-            if (!ss->closing && !ss->in_flight && !ss->queue.empty() && st == YAS_OK) {
+            if (!ss->closing && !ss->suspended && !ss->in_flight && !ss->queue.empty() && st == YAS_OK) {
                 st = session_needs_init(ss->s) ? launch_first(ss) : launch_pre_frame(ss);
                 launched = true;
             }
@@ -341,6 +342,53 @@ YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *c
     ss->id = (int)srv->sessions.size();
     srv->sessions.push_back(ss);
     *out_id = ss->id;
+    return YAS_OK;
+}
+
+// Session eviction and resumption (MapStruct::Hibernate / ReActivate,
+// VoxelMap.cu:894-954): the map's device arrays go to host memory and back.
+YAS_API int yas_server_suspend_session(yas_server *srv, int id) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    ServedSession *ss = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(srv->mu);
+        if (id < 0 || id >= (int)srv->sessions.size() || !srv->sessions[id]) return YAS_ERR_BAD_ARG;
+        ss = srv->sessions[id];
+        if (ss->suspended) return YAS_OK;
+        ss->suspended = true;  // the worker starts no new frame of it
+        srv->cv.wait(lk, [&] { return !ss->in_flight || srv->stop.load(); });
+    }
+    cudaSetDevice(srv->device);
+    YAS_TRY_CUDA(cudaStreamSynchronize(session_stream(ss->s)));
+    yas_map *m = nullptr;
+    YAS_TRY(yas_session_map(ss->s, &m));
+    return yas_map_hibernate(m);
+}
+
+YAS_API int yas_server_resume_session(yas_server *srv, int id) {
+    if (!srv) return YAS_ERR_BAD_ARG;
+    ServedSession *ss = nullptr;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        if (id < 0 || id >= (int)srv->sessions.size() || !srv->sessions[id]) return YAS_ERR_BAD_ARG;
+        ss = srv->sessions[id];
+        if (!ss->suspended) return YAS_OK;
+    }
+    cudaSetDevice(srv->device);
+    yas_map *m = nullptr;
+    YAS_TRY(yas_session_map(ss->s, &m));
+    // admission: the map's arrays must fit the free HBM minus the reserve
+    size_t free_b = 0, total_b = 0;
+    YAS_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t vb = m->cfg.voxel_format == YAS_VOXEL_F32 ? 8 : 4;
+    const size_t need = (size_t)m->cfg.hash_slots * sizeof(HashSlot) + (size_t)m->cfg.max_blocks * (12 + kBlockVoxels * vb);
+    if (free_b < need + srv->cfg.hbm_reserve_bytes) return YAS_ERR_OOM;
+    YAS_TRY(yas_map_reactivate(m));
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        ss->suspended = false;
+    }
+    srv->cv.notify_all();
     return YAS_OK;
 }
 

@@ -138,6 +138,9 @@ struct yas_session {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     cudaGraphExec_t pre_exec[2] = {nullptr, nullptr};  // served frames: up to the GN schedule
     cudaGraphExec_t post_exec = nullptr;               // served frames: after it
+    // the map's device arrays when the graphs were captured: growth, fusion
+    // into this map and hibernation move them, and the graphs are captured again
+    const void *graph_arrays[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // second stream of a tracked frame: the raycast branch runs beside the
     // pyramids of the new frame (fork/join events, captured as graph branches)
     cudaStream_t side = nullptr;
@@ -304,7 +307,27 @@ int session_copy_input(yas_session *s, const uint8_t *rgb, const uint16_t *depth
 
 bool session_needs_init(const yas_session *s) { return s->frames == 0; }
 
+// Drops captured graphs that name map arrays which have since moved; a
+// hibernated map cannot run frames.
+static int check_graphs(yas_session *s) {
+    if (s->map->hibernated) return YAS_ERR_STATE;
+    const void *now[5] = {s->map->slots, s->map->block_keys, s->map->voxels, s->map->visible, s->map->hdr};
+    bool same = true;
+    for (int i = 0; i < 5; ++i) same = same && now[i] == s->graph_arrays[i];
+    if (same) return YAS_OK;
+    for (int i = 0; i < 2; ++i) {
+        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
+        s->exec[i] = s->pre_exec[i] = nullptr;
+    }
+    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
+    s->post_exec = nullptr;
+    for (int i = 0; i < 5; ++i) s->graph_arrays[i] = now[i];
+    return YAS_OK;
+}
+
 int session_launch_first(yas_session *s) {
+    YAS_TRY(check_graphs(s));
     enqueue_first_frame(s);
     YAS_TRY_CUDA(cudaGetLastError());
     s->frames++;
@@ -312,6 +335,7 @@ int session_launch_first(yas_session *s) {
 }
 
 int session_launch_pre(yas_session *s) {
+    YAS_TRY(check_graphs(s));
     const int parity = s->tr->cur;
     if (!s->pre_exec[parity]) YAS_TRY(capture_graph(s, enqueue_pre, &s->pre_exec[parity], nullptr));
     YAS_TRY_CUDA(cudaGraphLaunch(s->pre_exec[parity], s->stream));
@@ -319,6 +343,7 @@ int session_launch_pre(yas_session *s) {
 }
 
 int session_launch_post(yas_session *s) {
+    YAS_TRY(check_graphs(s));
     if (!s->post_exec) YAS_TRY(capture_graph(s, enqueue_post, &s->post_exec, nullptr));
     YAS_TRY_CUDA(cudaGraphLaunch(s->post_exec, s->stream));
     s->tr->cur = 1 - s->tr->cur;
@@ -445,6 +470,7 @@ YAS_API int yas_session_destroy(yas_session *s) {
 
 YAS_API int yas_session_submit(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device) {
     if (!s || !rgb || !depth) return YAS_ERR_BAD_ARG;
+    YAS_TRY(check_graphs(s));
     const size_t n = (size_t)s->cfg.width * s->cfg.height;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
@@ -498,6 +524,38 @@ YAS_API int yas_session_raycaster(yas_session *s, yas_raycaster **out) {
     return YAS_OK;
 }
 
+YAS_API int yas_session_new_submap(yas_session *s, yas_map **out_previous) {
+    if (!s || !out_previous) return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->side) YAS_TRY_CUDA(cudaStreamSynchronize(s->side));
+    // camera pose in the world: T_world_map * Tcm of the last frame
+    yas_pose Tw, Tcm;
+    YAS_TRY(yas_map_get_pose(s->map, &Tw));
+    for (int i = 0; i < 12; ++i) Tcm.m[i] = s->fs_host->Tcm[i];
+    const Pose64 Tworld_cam = pose_mul(pose_from(Tw), pose_from(Tcm));
+    yas_map *nm = nullptr;
+    YAS_TRY(yas_map_create(&nm, &s->cfg.map, &s->cfg.K, s->stream));
+    const yas_pose Tn = pose_to(Tworld_cam);
+    yas_map_set_pose(nm, &Tn);
+    yas_map_set_active(s->map, 0);
+    *out_previous = s->map;
+    s->map = nm;
+    // captured frames name the previous map's arrays: capture again
+    for (int i = 0; i < 2; ++i) {
+        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
+        s->exec[i] = s->pre_exec[i] = nullptr;
+    }
+    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
+    s->post_exec = nullptr;
+    // the frame's pose relative to the new submap restarts at the identity
+    frame_begin_kernel<<<1, 32, 0, s->stream>>>(s->fs, pose_identity(), nm->hdr);
+    YAS_TRY_CUDA(cudaGetLastError());
+    YAS_TRY_CUDA(cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, s->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(s->stream));
+    return YAS_OK;
+}
+
 YAS_API int yas_session_frame_count(yas_session *s, int *out) {
     if (!s || !out) return YAS_ERR_BAD_ARG;
     *out = s->frames;
@@ -523,6 +581,7 @@ YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const 
                                       int *stage_ids, float *stage_ms, int capacity, int *out_count) {
     if (!s || !rgb || !depth || !out_count) return YAS_ERR_BAD_ARG;
     if (s->frames == 0) return YAS_ERR_STATE;  // the first frame initialises, it is not a tracked frame
+    YAS_TRY(check_graphs(s));
     const size_t n = (size_t)s->cfg.width * s->cfg.height;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));

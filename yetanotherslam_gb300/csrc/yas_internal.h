@@ -139,7 +139,7 @@ struct yas_map {
     bool active = true;
     std::mutex active_mutex;
     bool hibernated = false;
-    std::vector<unsigned char> hib_slots, hib_keys, hib_voxels;
+    std::vector<unsigned char> hib_slots, hib_keys, hib_voxels, hib_visible;
     yas::MapHeader hib_hdr;
     size_t voxel_bytes() const {
         return (size_t)cfg.max_blocks * yas::kBlockVoxels * (cfg.voxel_format == YAS_VOXEL_F32 ? 8 : 4);

@@ -90,6 +90,8 @@ void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *inv
                         float4 *nmap, cudaStream_t s);
 void launch_model_level(const float4 *prev, int pw, int w, int h, float4 *vmap, float4 *nmap,
                         cudaStream_t s);
+void launch_render_scene(const float4 *vmap, const float4 *nmap, int vpitch, int w, int h, float3 light,
+                         uchar4 *out, int opitch, cudaStream_t s);
 
 }  // namespace yas
 

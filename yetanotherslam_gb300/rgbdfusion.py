@@ -124,6 +124,13 @@ class MapStruct:
     def Reserve(self, hash_slots: int, max_blocks: int) -> None:
         L.call("yas_map_reserve", self.handle, hash_slots, max_blocks)
 
+    # MapStruct::SaveToFile / ReadFromFile
+    def SaveToFile(self, path: str) -> None:
+        L.call("yas_map_save", self.handle, str(path).encode())
+
+    def ReadFromFile(self, path: str) -> None:
+        L.call("yas_map_load", self.handle, str(path).encode())
+
     def Defuse(self, depth, Tcm) -> None:
         """Removes the observation of `depth` at Tcm (re-integration after a pose correction)."""
         ptr, pitch, dev, keep = _device_info(depth)
@@ -451,4 +458,16 @@ class Session:
         m.truncationDist = self.cfg.map.trunc_dist
         m._borrowed = True
         m.Release = lambda: None
+        return m
+
+    def new_submap(self) -> MapStruct:
+        """CreateNewKeyFrame's submap switch: returns the previous submap (owned by the caller)."""
+        h = C.c_void_p()
+        L.call("yas_session_new_submap", self.handle, C.byref(h))
+        m = MapStruct.__new__(MapStruct)
+        m.handle = h
+        m.K = self.cfg.K
+        m._stream = None
+        m.voxelSize = self.cfg.map.voxel_size
+        m.truncationDist = self.cfg.map.trunc_dist
         return m

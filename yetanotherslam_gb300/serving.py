@@ -32,6 +32,13 @@ class Server:
         self._sizes[sid.value] = (width, height)
         return sid.value
 
+    def suspend(self, sid: int) -> None:
+        """Moves the session's map to host memory (its frames wait until resume)."""
+        L.call("yas_server_suspend_session", self.handle, sid)
+
+    def resume(self, sid: int) -> None:
+        L.call("yas_server_resume_session", self.handle, sid)
+
     def close_session(self, sid: int) -> None:
         L.call("yas_server_close_session", self.handle, sid)
         self._sizes.pop(sid, None)
