@@ -154,6 +154,10 @@ YAS_API int yas_map_reserve(yas_map *map, int hash_slots, int max_blocks);
  * size (YAS_ERR_BAD_ARG otherwise); the round trip is bit-exact. */
 YAS_API int yas_map_save(yas_map *map, const char *path);
 YAS_API int yas_map_load(yas_map *map, const char *path);
+/* MapStruct::Swap(MapStruct*), VoxelMap.cu:173-199: the two maps exchange
+ * their storage, grid configuration, intrinsics and hibernation state; each
+ * handle keeps its pose and active flag, as in the reference. */
+YAS_API int yas_map_swap(yas_map *map, yas_map *other);
 /* MapStruct::Fuse(MapStruct *src), VoxelMap.cu:398-444 (System::FuseAllMapStruct,
  * System.cpp:73-93): fuses src into map using both maps' poses (yas_map_get_pose);
  * an empty map takes src's storage and pose.  src is left empty (the reference

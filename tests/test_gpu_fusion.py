@@ -146,3 +146,36 @@ def test_defuse_matches_oracle_and_undoes_a_frame(cuda):
             assert np.abs(sg[i][obs] - sr[j][obs]).max() <= 1e-5
         checked += 1
     assert checked == len(b0)
+
+
+def test_swap_exchanges_storage_not_pose(cuda):
+    """MapStruct::Swap (VoxelMap.cu:173-199): storage, grid and intrinsics
+    change hands; each handle keeps its pose and active flag."""
+    W, H = 160, 120
+    K = synth.intrinsics(W, H)
+    seq = sequence(5, 3, W, H)
+    TA = np.eye(4)
+    TB = np.eye(4)
+    TB[:3, 3] = [0.5, 0.0, -0.25]
+    a, _ = _build(seq, [0, 1], K, TA)
+    b = rf.MapStruct(K)
+    b.create_config(1 << 16, 1 << 14, 0.01, 0.03, rf.VOXEL_F16)
+    b.SetPose(TB)
+    b.SetActiveFlag(False)
+    ea = a.export()
+    a.Swap(b)
+    assert a.Empty() and not b.Empty()
+    for x, y in zip(b.export(), ea):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a.GetPose(), TA) and np.array_equal(b.GetPose(), TB)
+    assert a.isActive() and not b.isActive()
+    # the grid moved with the storage: a now fuses as a 10 mm F16 map
+    _, _, dm, Twc = seq[2]
+    a.Fuse(dm, Twc)
+    c, _, _ = a.export()
+    ref = rf.MapStruct(K)
+    ref.create_config(1 << 16, 1 << 14, 0.01, 0.03, rf.VOXEL_F16)
+    ref.Fuse(dm, Twc)
+    rc, _, _ = ref.export()
+    assert a.take_errors() == 0 and ref.take_errors() == 0
+    assert set(map(tuple, c.tolist())) == set(map(tuple, rc.tolist()))

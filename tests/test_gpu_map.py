@@ -231,3 +231,19 @@ def test_submap_file_roundtrip(cuda, fmt, tmp_path):
     with pytest.raises(L.YasError) as e:
         b.ReadFromFile(tmp_path / "missing.yas")
     assert e.value.code == 13
+    before = b.export()
+    raw = path.read_bytes()
+    (tmp_path / "short.yas").write_bytes(raw[:-7])
+    with pytest.raises(L.YasError) as e:
+        b.ReadFromFile(tmp_path / "short.yas")
+    assert e.value.code == 13
+    # a header whose block count does not match the file's length
+    bad = bytearray(raw)
+    bad[44:48] = (0xFFFFFFF0).to_bytes(4, "little")
+    (tmp_path / "big.yas").write_bytes(bytes(bad))
+    with pytest.raises(L.YasError) as e:
+        b.ReadFromFile(tmp_path / "big.yas")
+    assert e.value.code == 13
+    # the refused loads left b as it was
+    for x, y in zip(b.export(), before):
+        assert np.array_equal(x, y)

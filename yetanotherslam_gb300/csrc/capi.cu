@@ -603,6 +603,14 @@ YAS_API int yas_map_load(yas_map *m, const char *path) {
     std::vector<int32_t> coords;
     std::vector<unsigned char> vox;
     if (ok) {
+        // the block count is checked against the file's length before it sizes anything
+        const long here = ftell(f);
+        ok = here >= 0 && fseek(f, 0, SEEK_END) == 0;
+        const long end = ok ? ftell(f) : -1;
+        ok = ok && end >= here && fseek(f, here, SEEK_SET) == 0 && h.n_blocks <= (1u << 30) &&
+             (unsigned long long)(end - here) == (unsigned long long)h.n_blocks * (12ull + vb);
+    }
+    if (ok) {
         coords.resize((size_t)h.n_blocks * 3);
         vox.resize((size_t)h.n_blocks * vb);
         if (h.n_blocks)
@@ -673,6 +681,26 @@ YAS_API int yas_render_scene(const float *dev_vmap, const float *dev_nmap, int w
 // Grows the map to at least `want_slots` (power of two) slots and `want_blocks`
 // pool blocks; blocks keep their pool indices and contents, the table is
 // rebuilt.  The sticky error bits of earlier calls are kept.
+// Exchanges everything MapStruct::Swap exchanges (VoxelMap.cu:173-199): the
+// device storage, its configuration, the intrinsics and the hibernation state.
+// Pose and active flag stay with the handle.  Both streams must be idle.
+static void swap_storage(yas_map *a, yas_map *b) {
+    std::swap(a->cfg, b->cfg);
+    std::swap(a->cam_K, b->cam_K);
+    std::swap(a->slots, b->slots);
+    std::swap(a->slot_mask, b->slot_mask);
+    std::swap(a->block_keys, b->block_keys);
+    std::swap(a->voxels, b->voxels);
+    std::swap(a->visible, b->visible);
+    std::swap(a->hdr, b->hdr);
+    std::swap(a->hibernated, b->hibernated);
+    std::swap(a->hib_slots, b->hib_slots);
+    std::swap(a->hib_keys, b->hib_keys);
+    std::swap(a->hib_voxels, b->hib_voxels);
+    std::swap(a->hib_visible, b->hib_visible);
+    std::swap(a->hib_hdr, b->hib_hdr);
+}
+
 static int map_grow(yas_map *m, long long want_slots, long long want_blocks) {
     YAS_TRY(read_header(m));
     const unsigned n = std::min(m->hdr_host->n_alloc, (unsigned)m->cfg.max_blocks);
@@ -737,6 +765,15 @@ YAS_API int yas_map_reserve(yas_map *m, int hash_slots, int max_blocks) {
     return map_grow(m, hash_slots, max_blocks);
 }
 
+YAS_API int yas_map_swap(yas_map *a, yas_map *b) {
+    if (!a || !b) return YAS_ERR_BAD_ARG;
+    if (a == b) return YAS_OK;
+    YAS_TRY_CUDA(cudaStreamSynchronize(a->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    swap_storage(a, b);
+    return YAS_OK;
+}
+
 YAS_API int yas_map_fuse_map(yas_map *dst, yas_map *src) {
     if (!dst || !src || dst == src) return YAS_ERR_BAD_ARG;
     if (dst->hibernated || src->hibernated) return YAS_ERR_STATE;
@@ -750,20 +787,14 @@ YAS_API int yas_map_fuse_map(yas_map *dst, yas_map *src) {
     if (ndst == 0) {
         // Swap: the destination takes the source's storage, configuration and
         // pose; the source is left with the empty storage.
-        std::swap(dst->cfg, src->cfg);
-        std::swap(dst->slots, src->slots);
-        std::swap(dst->slot_mask, src->slot_mask);
-        std::swap(dst->block_keys, src->block_keys);
-        std::swap(dst->voxels, src->voxels);
-        std::swap(dst->visible, src->visible);
-        std::swap(dst->hdr, src->hdr);
-        std::lock_guard<std::mutex> a(dst->pose_mutex), b(src->pose_mutex);
+        swap_storage(dst, src);
+        std::scoped_lock lk(dst->pose_mutex, src->pose_mutex);
         std::swap(dst->Tcw, src->Tcw);
         return YAS_OK;
     }
     Pose64 Td, Ts;
     {
-        std::lock_guard<std::mutex> a(dst->pose_mutex), b(src->pose_mutex);
+        std::scoped_lock lk(dst->pose_mutex, src->pose_mutex);
         Td = dst->Tcw;
         Ts = src->Tcw;
     }

@@ -120,6 +120,10 @@ class MapStruct:
     def FuseMap(self, src: "MapStruct") -> None:
         L.call("yas_map_fuse_map", self.handle, src.handle)
 
+    # MapStruct::Swap(MapStruct*): exchange storage; each keeps its pose and flag
+    def Swap(self, other: "MapStruct") -> None:
+        L.call("yas_map_swap", self.handle, other.handle)
+
     # MapStruct::Reserve(hashTableSize, bucketSize, voxelBlockSize)
     def Reserve(self, hash_slots: int, max_blocks: int) -> None:
         L.call("yas_map_reserve", self.handle, hash_slots, max_blocks)
