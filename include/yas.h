@@ -115,6 +115,10 @@ YAS_API int yas_map_check_visible(yas_map *map, int cols, int rows, const yas_po
                                   unsigned *out_count);
 /* MapStruct::GetNumVisibleBlocks(): VoxelMap.h:58 / VoxelMap.cu:201-206. */
 YAS_API int yas_map_num_visible(yas_map *map, unsigned *out_count);
+/* MapStruct::ResetNumVisibleBlocks / ResetVisibleBlocks: VoxelMap.cu:208-211,963-966
+ * (the visible-block count drops to 0; the next raycast then starts from an
+ * empty visible set until the next fusion or visibility check). */
+YAS_API int yas_map_reset_visible(yas_map *map);
 /* Number of allocated blocks (no reference counterpart; heap pointer). */
 YAS_API int yas_map_num_allocated(yas_map *map, unsigned *out_count);
 /* Sticky device error bits of the map (YAS_ERR_* as 1<<code), cleared on read. */
@@ -293,6 +297,13 @@ typedef struct yas_gn_level {
  * enqueues work on `stream` (NULL: legacy default stream). */
 YAS_API int yas_gn_linearise_static(const yas_gn_level *level, const yas_pose *T, int mode, double *dev_out,
                                     void *stream);
+
+/* ---------------------------------------------------------------- copies
+ * No counterpart in the reference (which downloads cv::cuda::GpuMat): copies a
+ * pitched 2-D region, `height` rows of `width_bytes`, from host or device
+ * memory into host memory and waits for it, so host code can read the
+ * library's device buffers without linking the CUDA runtime itself. */
+YAS_API int yas_copy_to_host(void *dst, int dst_pitch, const void *src, int src_pitch, int width_bytes, int height);
 
 /* ---------------------------------------------------------------- shading
  * RenderScene(vmap, nmap, image), ImageProc.cu:128-139 (ImageProc.h:17): Phong

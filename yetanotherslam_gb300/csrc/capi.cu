@@ -308,6 +308,14 @@ YAS_API int yas_map_num_visible(yas_map *m, unsigned *out) {
     return YAS_OK;
 }
 
+YAS_API int yas_map_reset_visible(yas_map *m) {
+    if (!m) return YAS_ERR_BAD_ARG;
+    if (m->hibernated) return YAS_ERR_STATE;
+    YAS_TRY_CUDA(cudaMemsetAsync(&m->hdr->n_visible, 0, sizeof(unsigned), m->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    return YAS_OK;
+}
+
 YAS_API int yas_map_num_allocated(yas_map *m, unsigned *out) {
     if (!m || !out) return YAS_ERR_BAD_ARG;
     if (m->hibernated) {
@@ -648,6 +656,14 @@ YAS_API int yas_map_load(yas_map *m, const char *path) {
 
 // ------------------------------------------------------------------ shading
 extern "C" {
+
+YAS_API int yas_copy_to_host(void *dst, int dpitch, const void *src, int spitch, int width_bytes, int height) {
+    if (!dst || !src || width_bytes <= 0 || height <= 0 || dpitch < width_bytes || spitch < width_bytes)
+        return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaMemcpy2D(dst, (size_t)dpitch, src, (size_t)spitch, (size_t)width_bytes, (size_t)height,
+                              cudaMemcpyDefault));
+    return YAS_OK;
+}
 
 YAS_API int yas_render_scene(const float *dev_vmap, const float *dev_nmap, int width, int height, int pitch_bytes,
                              const float *light, uint8_t *rgba, int out_pitch_bytes, int on_device, void *stream) {

@@ -151,6 +151,9 @@ class MapStruct:
         L.call("yas_map_num_visible", self.handle, C.byref(out))
         return out.value
 
+    def ResetNumVisibleBlocks(self) -> None:
+        L.call("yas_map_reset_visible", self.handle)
+
     def num_allocated(self) -> int:
         out = C.c_uint()
         L.call("yas_map_num_allocated", self.handle, C.byref(out))
