@@ -247,6 +247,14 @@ YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int
  * pixel passes of every iteration separately.  Results agree within the
  * rounding of a different summation order. */
 YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused);
+/* How the Gauss-Newton sums are totalled across the GPU.  1 (default):
+ * compensated FP32 (TwoSum) partial sums with FP64 totals.  0: plain FP32
+ * sums in the same order, the reference's arithmetic (WarpReduceSum /
+ * BlockReduceSum and cv::cuda::reduce in FP32, TrackingUtils.h:8-58,
+ * RGBDTracking.cu:253-286), for precision comparisons.  The solve is FP64
+ * either way.  Takes effect at the next GetTransform, captured graphs
+ * included. */
+YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated);
 /* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);

@@ -221,6 +221,7 @@ class Session:
         self.hdl = self.L.orc_session_create(w, h, _ptr(_kvec(K)), voxel_size, trunc, levels, _ptr(it), mode,
                                              depth_scale, max_step)
         self.w, self.h = w, h
+        self.K = K
 
     def __del__(self):
         if getattr(self, "hdl", None):
@@ -235,6 +236,26 @@ class Session:
         T = np.eye(4)
         T[:3, :4] = out.reshape(3, 4)
         return st, T
+
+    def map_raycast(self, Tcm):
+        """Raycast of the session's map at Tcm (the model the next frame tracks against)."""
+        m = Map.__new__(Map)
+        m.L = self.L
+        m.h = self.L.orc_session_map(self.hdl)
+        try:
+            return m.raycast(self.w, self.h, self.K, Tcm)[0]
+        finally:
+            m.h = None
+
+    def map_mesh(self, cap: int = 4_000_000):
+        """Marching cubes of the session's map (Map.mesh)."""
+        m = Map.__new__(Map)
+        m.L = self.L
+        m.h = self.L.orc_session_map(self.hdl)
+        try:
+            return m.mesh(cap)
+        finally:
+            m.h = None
 
     def map_export(self):
         m = Map.__new__(Map)

@@ -1,0 +1,56 @@
+"""Precision variants against the FP64 oracle on a short sequence
+(tests/precision_study.py runs the full 300-frame, 640x480 / 5 mm study).
+
+Bars:
+  * per-frame tracking, open loop (the GPU tracker given the oracle's inputs
+    of each frame): the motion estimate within 1e-4 m and 1e-4 rad of the
+    oracle's with compensated sums, 1e-3 with plain sums;
+  * sessions (closed loop through their own maps): pose within 1e-4 m and 1e-4 rad of the oracle's on every frame
+    with compensated sums (the library's default), FP32 and FP16 TSDF alike;
+    plain FP32 sums (the reference's arithmetic) are held only to 1e-3, since
+    a rounding difference can flip GetTransform's keep-the-better-estimate
+    decision and move a frame by more than 1e-4;
+  * mapping with the oracle's poses: weights exactly equal; TSDF (normalised
+    by the truncation) within 1e-5 for FP32 and S24 storage; marching cubes
+    with the oracle's case index on at least 99.99 % of cubes and vertices
+    within 1e-4 of a voxel at the 99th percentile;
+  * FP16 storage rounds every running-average write to an 11-bit mantissa
+    (ulp 2^-11 near |sdf| = 1), and those errors add up like a random walk
+    over the observations, about ulp/sqrt(12) * sqrt(n/3) per voxel; over
+    these <= 24 observations the bar is 5e-3 (max) and 1.5e-3 (99th
+    percentile), 99.9 % of cubes with the oracle's case and vertices within
+    5e-3 of a voxel at the 99th percentile.
+"""
+from __future__ import annotations
+
+import pytest
+
+from tests import precision_study as ps
+
+pytestmark = pytest.mark.gpu
+
+
+def test_precision_variants_against_oracle(cuda):
+    vs = 0.008
+    rep = ps.run(frames=24, W=320, H=240, voxel=vs, seed=11, mc_every=12, slots=1 << 19, blocks=1 << 16,
+                 log=lambda *_: None)
+    bad = []
+    for red, p in rep["open_loop_vs_oracle"].items():
+        bar = {"comp": 1e-4, "plain": 1e-3, "oracle_f64": 1e-7, "oracle_f32": 1e-3}[red]  # 1e-7: the arccos floor
+        if not (p["t_m"]["max"] <= bar and p["r_rad"]["max"] <= bar and p["t_m"]["n"] == 23):
+            bad.append(("open loop", red, p["t_m"]["max"], p["r_rad"]["max"]))
+    for name, p in rep["pose_vs_oracle"].items():
+        bar = 1e-4 if name.endswith("comp") else 1e-3
+        if not (p["t_m"]["max"] <= bar and p["r_rad"]["max"] <= bar):
+            bad.append(("pose", name, p["t_m"]["max"], p["r_rad"]["max"]))
+    for chk in rep["checks"]:
+        for f, v in chk["mapping"].items():
+            tsdf_bar, p99_bar, case_bar, vert_bar = ((5e-3, 1.5e-3, 0.999, 5e-3) if f == "f16" else
+                                                     (1e-5, 1e-5, 0.9999, 1e-4))
+            t, m = v["tsdf"], v["mesh"]
+            if not (t["weight_equal_frac"] == 1.0 and t["max"] <= tsdf_bar and t["p99"] <= p99_bar
+                    and t["n"] > 100000):
+                bad.append(("tsdf", chk["frame"], f, t["max"], t["weight_equal_frac"], t["n"]))
+            if not (m["same_case_frac"] >= case_bar and m["p99"] <= vert_bar * vs):
+                bad.append(("mesh", chk["frame"], f, m["same_case_frac"], m["p99"], m["max"]))
+    assert not bad, (bad, ps.summary(rep))

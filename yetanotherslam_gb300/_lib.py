@@ -114,6 +114,7 @@ _SIGS = {
     "yas_map_swap": [_P, _P],
     "yas_map_reset_visible": [_P],
     "yas_copy_to_host": [_P, _I, _P, _I, _I, _I],
+    "yas_tracker_set_reduction": [_P, _I],
     "yas_map_defuse_depth": [_P, _P, _I, _I, _I, _I, C.POINTER(Pose)],
     "yas_raycaster_create": [_PP, _I, _I, C.POINTER(Intrinsics), _P],
     "yas_raycaster_destroy": [_P],

@@ -1209,6 +1209,14 @@ YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused) {
     return YAS_OK;
 }
 
+YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated) {
+    if (!tr) return YAS_ERR_BAD_ARG;
+    const unsigned plain = compensated ? 0u : 1u;
+    YAS_TRY_CUDA(cudaMemcpyAsync(&tr->state->plain_sums, &plain, sizeof(plain), cudaMemcpyHostToDevice, tr->stream));
+    YAS_TRY_CUDA(cudaStreamSynchronize(tr->stream));
+    return YAS_OK;
+}
+
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out) {
     if (!tr || !out) return YAS_ERR_BAD_ARG;
     *out = tr->good ? 1 : 0;

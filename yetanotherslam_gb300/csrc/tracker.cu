@@ -126,7 +126,7 @@ __device__ __forceinline__ void cta_row32(float v[32], float *row) {
 // last to arrive folds the group's rows (compensated FP32) into the (hi, lo)
 // row grow[g], resets the ticket and returns true.
 __device__ __forceinline__ bool group_fold(const float *rows, float *grow, unsigned *ticket, unsigned cta,
-                                           unsigned nact) {
+                                           unsigned nact, bool plain) {
     constexpr unsigned S = kSubsets;
     __shared__ float wsum[S][32];
     __shared__ float lsum[S][32];
@@ -167,7 +167,7 @@ __device__ __forceinline__ bool group_fold(const float *rows, float *grow, unsig
             l += e + lsum[k][c];
         }
         grow[g * 64 + c] = h;
-        grow[g * 64 + 32 + c] = l;
+        grow[g * 64 + 32 + c] = plain ? 0.0f : l;  // plain: the same order, no error terms
     }
     if (threadIdx.x == 0) atomicExch(&ticket[g], 0u);
     __threadfence();
@@ -178,7 +178,8 @@ __device__ __forceinline__ bool group_fold(const float *rows, float *grow, unsig
 // Stage 3: a group folder takes the grid ticket; the last of the `ngroups`
 // folds the group rows (compensated FP32 per subset, subsets added in FP64)
 // into tot[0..31] (shared), resets the ticket and returns true.
-__device__ __forceinline__ bool grid_fold(const float *grow, unsigned *ticket, unsigned ngroups, double *tot) {
+__device__ __forceinline__ bool grid_fold(const float *grow, unsigned *ticket, unsigned ngroups, double *tot,
+                                          bool plain) {
     constexpr unsigned S = kSubsets;
     __shared__ double dsum[S][32];
     __shared__ bool flag;
@@ -202,14 +203,21 @@ __device__ __forceinline__ bool grid_fold(const float *grow, unsigned *ticket, u
             h = s;
             l += e + xl1;
         }
-        dsum[sub][c] = (double)h + (double)l;
+        dsum[sub][c] = plain ? (double)h : (double)h + (double)l;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
-        double s = 0.0;
+        if (plain) {
+            float s = 0.0f;
 #pragma unroll
-        for (unsigned k = 0; k < S; ++k) s += dsum[k][threadIdx.x];
-        tot[threadIdx.x] = s;
+            for (unsigned k = 0; k < S; ++k) s += (float)dsum[k][threadIdx.x];
+            tot[threadIdx.x] = (double)s;
+        } else {
+            double s = 0.0;
+#pragma unroll
+            for (unsigned k = 0; k < S; ++k) s += dsum[k][threadIdx.x];
+            tot[threadIdx.x] = s;
+        }
     }
     if (threadIdx.x == 0) atomicExch(ticket, 0u);
     __syncthreads();
@@ -217,10 +225,10 @@ __device__ __forceinline__ bool grid_fold(const float *grow, unsigned *ticket, u
 }
 
 __device__ __forceinline__ bool grid_reduce32(float v[32], float *partial, float *grow, unsigned *counters,
-                                              double *tot) {
+                                              double *tot, bool plain) {
     cta_row32(v, partial + blockIdx.x * 32);
-    if (!group_fold(partial, grow, counters + 1, blockIdx.x, gridDim.x)) return false;
-    return grid_fold(grow, counters, (gridDim.x + kGroup - 1) / kGroup, tot);
+    if (!group_fold(partial, grow, counters + 1, blockIdx.x, gridDim.x, plain)) return false;
+    return grid_fold(grow, counters, (gridDim.x + kGroup - 1) / kGroup, tot, plain);
 }
 
 // ---------------------------------------------------------------- estimate helpers
@@ -360,7 +368,7 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
             }
         }
     }
-    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
+    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot, st->plain_sums != 0u)) return;
     if (threadIdx.x < 32) st->a_sums[threadIdx.x] = tot[threadIdx.x];
     if (threadIdx.x == 0) st->huber_th = huber_threshold(tot);
     if (a.mode == YAS_TRACK_ICP) {
@@ -414,7 +422,7 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_b(PassArgs a) {
                 for (int j = i; j < 7; ++j) acc[q++] += wt * row[i] * row[j];
         }
     }
-    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot)) return;
+    if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot, st->plain_sums != 0u)) return;
     load_solve_state(st);
     if (threadIdx.x < 32) {
         st->b_sums[threadIdx.x] = tot[threadIdx.x];
@@ -647,7 +655,7 @@ __device__ __forceinline__ void fused_publish_row(float v[32], unsigned long lon
 // into g_solve.A[29..31]; compensated FP32 per column (32 lanes x 5 rows,
 // then a butterfly), FP64 at the end.  False on abort or timeout.
 __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, unsigned nrows, unsigned tag,
-                                             GNState *st) {
+                                             GNState *st, bool plain) {
     __shared__ float m3[3][kFusedMaxCtas];
     const int t = (int)threadIdx.x;
     bool mine = true;
@@ -685,7 +693,7 @@ __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, uns
             h = s;
             l = (l + ol) + e;
         }
-        if (lane == 0) g_solve.A[29 + warp] = (double)h + (double)l;
+        if (lane == 0) g_solve.A[29 + warp] = plain ? (double)h : (double)h + (double)l;
     }
     __syncthreads();
     return true;
@@ -698,7 +706,8 @@ __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, uns
 // a butterfly over the 16 subsets of each column; FP64 at the end.  False on
 // abort or timeout.
 __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, const unsigned long long *rowsB,
-                                             unsigned nrows, unsigned tag, bool icp, bool rgb, GNState *st) {
+                                             unsigned nrows, unsigned tag, bool icp, bool rgb, GNState *st,
+                                             bool plain) {
     __shared__ float hs[kFoldSubsets][65], ls[kFoldSubsets][65];
     const int t = (int)threadIdx.x, c = t & 63, sub = t >> 6;
     const bool need = (c < 29 && icp) || (c >= 32 && c < 60 && rgb);
@@ -751,7 +760,7 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
             l2 = (l2 + ol) + e;
         }
         if (s_ == 0) {
-            const double v = (double)h2 + (double)l2;
+            const double v = plain ? (double)h2 : (double)h2 + (double)l2;
             if (col < 29) g_solve.A[col] = v;
             else if (col >= 32 && col < 60) g_solve.B[col - 32] = v;
         }
@@ -779,6 +788,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
         g_solve.B[t - 32] = 0.0;
     }
     const unsigned epoch = __ldcg(&st->epoch);
+    const bool plain = __ldcg(&st->plain_sums) != 0u;
     __syncthreads();
     unsigned s = 0u;
     bool alive = true;
@@ -821,7 +831,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             }
             fused_publish_row(acc, rA + cta * 32, tag);
             if (do_rgb) {
-                if (!fold_moments(rA, nrows, tag, st)) return;
+                if (!fold_moments(rA, nrows, tag, st, plain)) return;
                 if (t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
                 __syncthreads();
                 const float th = g_solve.huber_th;
@@ -846,7 +856,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                 }
                 fused_publish_row(acc, rB + cta * 32, tag);
             }
-            if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st)) return;
+            if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st, plain)) return;
             if (t < 32) {
                 if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
                 gn_solve(mode, 0, it == 0, l);
@@ -1253,6 +1263,8 @@ extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas
     cudaStream_t s = (cudaStream_t)stream;
     // tickets must start at zero; everything else is written before it is read
     YAS_TRY_CUDA(cudaMemsetAsync(sc->counters, 0, sizeof(sc->counters), s));
+    // compensated sums, whatever an earlier call left
+    YAS_TRY_CUDA(cudaMemsetAsync(&sc->state.plain_sums, 0, sizeof(unsigned), s));
     PassArgs a;
     memset(&a, 0, sizeof(a));
     a.c.fx = lv->fx;

@@ -359,6 +359,10 @@ class RGBDTracking:
         """Whole schedule in one cooperative launch (True) or two launches per iteration."""
         L.call("yas_tracker_set_schedule", self.handle, int(fused))
 
+    def set_reduction(self, compensated: bool) -> None:
+        """Compensated FP32 sums with FP64 totals (True) or plain FP32 sums (False)."""
+        L.call("yas_tracker_set_reduction", self.handle, int(compensated))
+
     def IsTrackingGood(self) -> bool:
         out = C.c_int()
         L.call("yas_tracker_is_good", self.handle, C.byref(out))
@@ -478,3 +482,10 @@ class Session:
         m.voxelSize = self.cfg.map.voxel_size
         m.truncationDist = self.cfg.map.trunc_dist
         return m
+
+    def set_reduction(self, compensated: bool) -> None:
+        """Gauss-Newton totals of the session's tracker: compensated FP32 with FP64
+        totals (True, the default) or plain FP32 sums (False)."""
+        h = C.c_void_p()
+        L.call("yas_session_tracker", self.handle, C.byref(h))
+        L.call("yas_tracker_set_reduction", h, int(compensated))
