@@ -384,6 +384,59 @@ YAS_API void *yas_session_stream(yas_session *s);
 YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const uint16_t *depth, int on_device,
                                       int *stage_ids, float *stage_ms, int capacity, int *out_count);
 
+/* ---------------------------------------------------------------- batched submaps
+ * No counterpart in the reference, which tracks and fuses one keyframe submap
+ * at a time (FullSystem/src/Tracking.cpp:162-197).  A batch steps many
+ * sessions together: keyframe submaps of any resolution and voxel size.  One
+ * step runs one frame of every active session as a single CUDA graph launch.
+ * The graph holds:
+ *   - each session's pyramids, raycast and model pyramid, as parallel branches;
+ *   - one persistent cooperative Gauss-Newton launch over all their pyramid
+ *     levels (split in two only if the CTAs exceed what is co-resident);
+ *   - each session's pose update and fusion (allocation, visibility,
+ *     integration).
+ * A graph is captured once per combination of the sessions' states (inactive,
+ * initialising, tracked on either frame-buffer parity) and then reused.  The
+ * sessions stay owned by the caller, who must not drive them by other calls
+ * while the batch steps them. */
+typedef struct yas_batch yas_batch;
+
+typedef struct yas_batch_tuning {
+    int march_warps_x;     /* ray-march CTA shape: 1 (8x16 px), 2 (16x8), 4 (32x4)     */
+    int integrate_ctas;    /* CTAs of the integration grid, 256 threads each          */
+    int gn_pixels_per_cta; /* batched GN: one 1024-thread CTA per this many level-0
+                            * pixels (1..16 CTAs per session); fixes each session's
+                            * summation order, so results depend on it, not on the mix */
+} yas_batch_tuning;
+
+/* Defaults: 2, 1216 (152 x 8), 32768. */
+YAS_API int yas_batch_tuning_default(yas_batch_tuning *t);
+YAS_API int yas_batch_create(yas_batch **out, yas_session *const *sessions, int count, void *stream);
+YAS_API int yas_batch_destroy(yas_batch *b);
+YAS_API int yas_batch_set_tuning(yas_batch *b, const yas_batch_tuning *t);
+YAS_API int yas_batch_get_tuning(yas_batch *b, yas_batch_tuning *out);
+/* Enqueues one frame of every session i with active[i] != 0 (active NULL: all).
+ * rgb[i] / depth[i] as for yas_session_submit (host memory must stay valid
+ * until yas_batch_wait returns).  Does not wait. */
+YAS_API int yas_batch_step(yas_batch *b, const uint8_t *const *rgb, const uint16_t *const *depth,
+                           const int *active, int on_device);
+/* Waits for the last step.  For every session it ran: its map pose and frame
+ * status (other entries are left as they are; either array may be NULL).
+ * out_ms (may be NULL): device time of the step, input copies included. */
+YAS_API int yas_batch_wait(yas_batch *b, yas_pose *out_Tcm, int *out_status, float *out_ms);
+/* Kernel nodes of the last step's graph. */
+YAS_API int yas_batch_kernels_per_step(yas_batch *b, int *out);
+/* The launch-shape autotuner.  It copies every session's configuration into
+ * scratch sessions and runs them through the first `frames` (>= 3) frames of
+ * each session: rgb[i] / depth[i] hold that many consecutive frames.  Each
+ * knob (GN share, march CTA shape, integration grid) is tried in turn over a
+ * few candidate values, the others held, each candidate timed by the median
+ * device time of its steps.  The fastest value is kept, applied to the batch
+ * and written to *out (may be NULL).  The batch's own sessions are not
+ * touched. */
+YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const uint16_t *const *depth, int frames,
+                               int on_device, yas_batch_tuning *out);
+
 /* ---------------------------------------------------------------- served sessions
  * No counterpart in the reference, which runs one session per process
  * (FullSystem/src/System.cpp:43-65).  A request server runs the frames of many

@@ -57,6 +57,10 @@ class ServerConfig(C.Structure):
     _fields_ = [("max_sessions", C.c_int), ("hbm_reserve_bytes", C.c_size_t), ("ring_frames", C.c_int)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("march_warps_x", C.c_int), ("integrate_ctas", C.c_int), ("gn_pixels_per_cta", C.c_int)]
+
+
 class ServedResult(C.Structure):
     _fields_ = [("session", C.c_int), ("status", C.c_int), ("frame", C.c_longlong), ("latency_ms", C.c_double),
                 ("Tcm", Pose)]
@@ -161,6 +165,15 @@ _SIGS = {
     "yas_mc_tables": [_P, _P, _P],
     "yas_render_scene": [_P, _P, _I, _I, _I, _P, _P, _I, _I, _P],
     "yas_gn_linearise_static": [C.POINTER(GnLevel), C.POINTER(Pose), _I, _P, _P],
+    "yas_batch_tuning_default": [C.POINTER(BatchTuning)],
+    "yas_batch_create": [_PP, _PP, _I, _P],
+    "yas_batch_destroy": [_P],
+    "yas_batch_set_tuning": [_P, C.POINTER(BatchTuning)],
+    "yas_batch_get_tuning": [_P, C.POINTER(BatchTuning)],
+    "yas_batch_step": [_P, _PP, _PP, _PI, _I],
+    "yas_batch_wait": [_P, C.POINTER(Pose), _PI, C.POINTER(C.c_float)],
+    "yas_batch_kernels_per_step": [_P, _PI],
+    "yas_batch_autotune": [_P, _PP, _PP, _I, _I, C.POINTER(BatchTuning)],
     "yas_server_config_default": [C.POINTER(ServerConfig)],
     "yas_server_create": [_PP, C.POINTER(ServerConfig)],
     "yas_server_destroy": [_P],

@@ -1,0 +1,468 @@
+// batch.cu — many keyframe submaps stepped as one CUDA graph, and the
+// launch-shape autotuner.
+//
+// The reference tracks and fuses one submap at a time, one kernel after the
+// other on the legacy stream (FullSystem/src/Tracking.cpp:162-197).  Here a
+// step of N sessions (submaps of any resolution and voxel size) is one graph:
+//
+//   fork -> per session: [ pyramids | raycast -> model pyramid ] -> GN reset
+//        -> one persistent cooperative Gauss-Newton launch (gn_fused_batch) in
+//           which every session owns a fixed share of CTAs and runs all its
+//           pyramid levels and iterations
+//        -> per session: pose update, allocation, visibility, integration
+//   join
+//
+// so the small per-session kernels of different submaps overlap on the SMs,
+// and the latency-bound GN schedule of all submaps costs one launch.  A graph
+// is captured per combination of session states (inactive, initialising,
+// tracked on frame-buffer parity 0 / 1): every pointer it names is fixed for
+// that combination, including the GN descriptors, which live in device memory
+// owned by the cached graph.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "yas_session.h"
+
+using namespace yas;
+
+namespace {
+
+enum : uint8_t { kIdle = 0, kFirst = 1, kTrack0 = 2, kTrack1 = 3 };
+
+struct CachedStep {
+    std::vector<uint8_t> key;
+    cudaGraphExec_t exec = nullptr;
+    GNBatchItem *d_items = nullptr;
+    unsigned short *d_map = nullptr;
+    int kernels = 0;
+    unsigned long long last_use = 0;
+};
+
+struct GNGroup {
+    int item0, nitems, cta0, nctas;
+};
+
+constexpr size_t kMaxCached = 8;
+
+}  // namespace
+
+struct yas_batch {
+    std::vector<yas_session *> s;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev_fork = nullptr, ev_gn = nullptr, ev_start = nullptr, ev_end = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_pre, ev_post;
+    yas_batch_tuning tuning;
+    std::vector<CachedStep> cache;
+    std::vector<const void *> arrays;  // every session's map arrays when the cache was filled
+    std::vector<uint8_t> last_key;
+    int last_kernels = 0;
+    unsigned long long clock = 0;
+    bool pending = false;
+};
+
+static LaunchShape shape_of(const yas_batch_tuning &t) {
+    LaunchShape sh;
+    sh.march_warps_x = t.march_warps_x;
+    sh.integrate_ctas = t.integrate_ctas;
+    sh.gn_pixels_per_cta = t.gn_pixels_per_cta;
+    return sh;
+}
+
+static bool tuning_valid(const yas_batch_tuning &t) {
+    return (t.march_warps_x == 1 || t.march_warps_x == 2 || t.march_warps_x == 4) && t.integrate_ctas > 0 &&
+           t.integrate_ctas <= (1 << 20) && t.gn_pixels_per_cta >= 1024;
+}
+
+static void free_cached(CachedStep &c) {
+    if (c.exec) cudaGraphExecDestroy(c.exec);
+    cudaFree(c.d_items);
+    cudaFree(c.d_map);
+    c.exec = nullptr;
+    c.d_items = nullptr;
+    c.d_map = nullptr;
+}
+
+static void clear_cache(yas_batch *b) {
+    for (CachedStep &c : b->cache) free_cached(c);
+    b->cache.clear();
+}
+
+// Drops the cached graphs once any session's map arrays have moved (growth,
+// fusion into it, hibernation, a loaded file).
+static int check_arrays(yas_batch *b) {
+    std::vector<const void *> now;
+    now.reserve(b->s.size() * 5);
+    for (yas_session *s : b->s) {
+        const yas_map *m = session_map_handle(s);
+        if (m->hibernated) return YAS_ERR_STATE;
+        now.insert(now.end(), {m->slots, m->block_keys, m->voxels, m->visible, m->hdr});
+    }
+    if (now != b->arrays) {
+        clear_cache(b);
+        b->arrays = now;
+    }
+    return YAS_OK;
+}
+
+static std::vector<uint8_t> step_key(const yas_batch *b, const int *active) {
+    std::vector<uint8_t> key(b->s.size(), kIdle);
+    for (size_t i = 0; i < b->s.size(); ++i) {
+        if (active && !active[i]) continue;
+        yas_session *s = b->s[i];
+        key[i] = session_needs_init(s) ? kFirst : (uint8_t)(kTrack0 + session_tracker(s)->cur);
+    }
+    return key;
+}
+
+static int count_kernels(cudaGraph_t g, int *out) {
+    size_t n = 0;
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    int k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        YAS_TRY_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    *out = k;
+    return YAS_OK;
+}
+
+// The GN descriptors of the tracked sessions, packed into cooperative launches
+// of at most `capacity` CTAs each (a session never straddles two).
+static int plan_gn(yas_batch *b, const std::vector<uint8_t> &key, std::vector<GNBatchItem> &items,
+                   std::vector<unsigned short> &cta_item, std::vector<GNGroup> &groups) {
+    const int capacity = gn_batch_capacity();
+    if (capacity <= 0) return YAS_ERR_STATE;  // no cooperative launch on this device
+    GNGroup g = {0, 0, 0, 0};
+    for (size_t i = 0; i < b->s.size(); ++i) {
+        if (key[i] < kTrack0) continue;
+        yas_tracker *tr = session_tracker(b->s[i]);
+        const int n = gn_batch_ctas(tr, b->tuning.gn_pixels_per_cta);
+        if (n > capacity) return YAS_ERR_CAPACITY;
+        if (g.nctas + n > capacity) {
+            groups.push_back(g);
+            g = {(int)items.size(), 0, (int)cta_item.size(), 0};
+        }
+        GNBatchItem it;
+        gn_batch_item(tr, g.nctas, &it, b->tuning.gn_pixels_per_cta);
+        for (int c = 0; c < it.nctas; ++c) cta_item.push_back((unsigned short)g.nitems);
+        items.push_back(it);
+        g.nitems += 1;
+        g.nctas += it.nctas;
+    }
+    if (g.nitems) groups.push_back(g);
+    return YAS_OK;
+}
+
+static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedStep &out) {
+    std::vector<GNBatchItem> items;
+    std::vector<unsigned short> cta_item;
+    std::vector<GNGroup> groups;
+    YAS_TRY(plan_gn(b, key, items, cta_item, groups));
+    out.key = key;
+    if (!items.empty()) {
+        if (cudaMalloc(&out.d_items, items.size() * sizeof(GNBatchItem)) != cudaSuccess ||
+            cudaMalloc(&out.d_map, cta_item.size() * sizeof(unsigned short)) != cudaSuccess) {
+            cudaGetLastError();
+            free_cached(out);
+            return YAS_ERR_OOM;
+        }
+        YAS_TRY_CUDA(cudaMemcpy(out.d_items, items.data(), items.size() * sizeof(GNBatchItem),
+                                cudaMemcpyHostToDevice));
+        YAS_TRY_CUDA(cudaMemcpy(out.d_map, cta_item.data(), cta_item.size() * sizeof(unsigned short),
+                                cudaMemcpyHostToDevice));
+    }
+    YAS_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaEventRecord(b->ev_fork, b->stream);
+    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
+        if (key[i] == kIdle) continue;
+        yas_session *s = b->s[i];
+        cudaStream_t st = session_stream(s);
+        err = cudaStreamWaitEvent(st, b->ev_fork, 0);
+        if (err != cudaSuccess) break;
+        if (key[i] == kFirst)
+            session_enqueue_first(s);
+        else
+            session_enqueue_pre(s);
+        err = cudaEventRecord(b->ev_pre[i], st);
+    }
+    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i)
+        if (key[i] >= kTrack0) err = cudaStreamWaitEvent(b->stream, b->ev_pre[i], 0);
+    for (const GNGroup &g : groups) {
+        if (err != cudaSuccess) break;
+        err = launch_gn_batch(out.d_items + g.item0, out.d_map + g.cta0, g.nctas, b->stream);
+    }
+    if (err == cudaSuccess && !groups.empty()) err = cudaEventRecord(b->ev_gn, b->stream);
+    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
+        if (key[i] < kTrack0) continue;
+        yas_session *s = b->s[i];
+        cudaStream_t st = session_stream(s);
+        err = cudaStreamWaitEvent(st, b->ev_gn, 0);
+        if (err != cudaSuccess) break;
+        session_enqueue_post(s);
+        err = cudaEventRecord(b->ev_post[i], st);
+    }
+    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
+        if (key[i] == kIdle) continue;
+        err = cudaStreamWaitEvent(b->stream, key[i] == kFirst ? b->ev_pre[i] : b->ev_post[i], 0);
+    }
+    if (err == cudaSuccess) err = cudaGetLastError();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (err == cudaSuccess) err = e2;
+    int st = YAS_OK;
+    if (err != cudaSuccess) {
+        record_cuda_error(err, "batch capture", __FILE__, __LINE__);
+        st = YAS_ERR_CUDA;
+    }
+    if (st == YAS_OK) st = count_kernels(g, &out.kernels);
+    if (st == YAS_OK && cudaGraphInstantiate(&out.exec, g, 0) != cudaSuccess) {
+        record_cuda_error(cudaGetLastError(), "batch instantiate", __FILE__, __LINE__);
+        st = YAS_ERR_CUDA;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (st != YAS_OK) free_cached(out);
+    return st;
+}
+
+static CachedStep *find_or_capture(yas_batch *b, const std::vector<uint8_t> &key, int *status) {
+    for (CachedStep &c : b->cache)
+        if (c.key == key) {
+            c.last_use = ++b->clock;
+            *status = YAS_OK;
+            return &c;
+        }
+    if (b->cache.size() >= kMaxCached) {
+        auto lru = std::min_element(b->cache.begin(), b->cache.end(),
+                                    [](const CachedStep &x, const CachedStep &y) { return x.last_use < y.last_use; });
+        free_cached(*lru);
+        b->cache.erase(lru);
+    }
+    CachedStep c;
+    *status = capture_step(b, key, c);
+    if (*status != YAS_OK) return nullptr;
+    c.last_use = ++b->clock;
+    b->cache.push_back(c);
+    return &b->cache.back();
+}
+
+static void apply_tuning(yas_batch *b, const yas_batch_tuning &t) {
+    b->tuning = t;
+    const LaunchShape sh = shape_of(t);
+    for (yas_session *s : b->s) session_set_shape(s, sh);
+    clear_cache(b);
+}
+
+extern "C" {
+
+YAS_API int yas_batch_tuning_default(yas_batch_tuning *t) {
+    if (!t) return YAS_ERR_BAD_ARG;
+    t->march_warps_x = 2;
+    t->integrate_ctas = 152 * 8;
+    t->gn_pixels_per_cta = 32768;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_destroy(yas_batch *b) {
+    if (!b) return YAS_ERR_BAD_ARG;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    clear_cache(b);
+    for (cudaEvent_t e : {b->ev_fork, b->ev_gn, b->ev_start, b->ev_end})
+        if (e) cudaEventDestroy(e);
+    for (auto *v : {&b->ev_in, &b->ev_pre, &b->ev_post})
+        for (cudaEvent_t e : *v)
+            if (e) cudaEventDestroy(e);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_create(yas_batch **out, yas_session *const *sessions, int count, void *stream) {
+    if (!out || !sessions || count <= 0 || count > 4096) return YAS_ERR_BAD_ARG;
+    for (int i = 0; i < count; ++i) {
+        if (!sessions[i]) return YAS_ERR_BAD_ARG;
+        for (int j = 0; j < i; ++j)
+            if (sessions[j] == sessions[i]) return YAS_ERR_BAD_ARG;
+    }
+    yas_batch *b = new yas_batch();
+    b->s.assign(sessions, sessions + count);
+    yas_batch_tuning_default(&b->tuning);
+    int st = YAS_OK;
+    if (stream) {
+        b->stream = static_cast<cudaStream_t>(stream);
+    } else if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess) {
+        b->own_stream = true;
+    } else {
+        st = YAS_ERR_CUDA;
+    }
+    auto mk = [&](cudaEvent_t *e, unsigned flags) {
+        if (st == YAS_OK && cudaEventCreateWithFlags(e, flags) != cudaSuccess) st = YAS_ERR_CUDA;
+    };
+    mk(&b->ev_fork, cudaEventDisableTiming);
+    mk(&b->ev_gn, cudaEventDisableTiming);
+    mk(&b->ev_start, cudaEventDefault);
+    mk(&b->ev_end, cudaEventDefault);
+    b->ev_in.assign(count, nullptr);
+    b->ev_pre.assign(count, nullptr);
+    b->ev_post.assign(count, nullptr);
+    for (int i = 0; i < count; ++i) {
+        mk(&b->ev_in[i], cudaEventDisableTiming);
+        mk(&b->ev_pre[i], cudaEventDisableTiming);
+        mk(&b->ev_post[i], cudaEventDisableTiming);
+    }
+    if (st != YAS_OK) {
+        cudaGetLastError();
+        yas_batch_destroy(b);
+        return st;
+    }
+    apply_tuning(b, b->tuning);
+    *out = b;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_set_tuning(yas_batch *b, const yas_batch_tuning *t) {
+    if (!b || !t || !tuning_valid(*t)) return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    apply_tuning(b, *t);
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_get_tuning(yas_batch *b, yas_batch_tuning *out) {
+    if (!b || !out) return YAS_ERR_BAD_ARG;
+    *out = b->tuning;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_step(yas_batch *b, const uint8_t *const *rgb, const uint16_t *const *depth,
+                           const int *active, int on_device) {
+    if (!b || !rgb || !depth) return YAS_ERR_BAD_ARG;
+    const std::vector<uint8_t> key = step_key(b, active);
+    for (size_t i = 0; i < key.size(); ++i)
+        if (key[i] != kIdle && (!rgb[i] || !depth[i])) return YAS_ERR_BAD_ARG;
+    YAS_TRY(check_arrays(b));
+    // the previous step's graph runs on b->stream: the copies below wait for it
+    YAS_TRY_CUDA(cudaEventRecord(b->ev_start, b->stream));
+    for (size_t i = 0; i < key.size(); ++i) {
+        if (key[i] == kIdle) continue;
+        yas_session *s = b->s[i];
+        YAS_TRY_CUDA(cudaStreamWaitEvent(session_stream(s), b->ev_start, 0));
+        YAS_TRY(session_copy_input(s, rgb[i], depth[i], on_device));
+        YAS_TRY_CUDA(cudaEventRecord(b->ev_in[i], session_stream(s)));
+        YAS_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in[i], 0));
+    }
+    int st = YAS_OK;
+    bool any = false;
+    for (uint8_t k : key) any = any || k != kIdle;
+    if (any) {
+        CachedStep *c = find_or_capture(b, key, &st);
+        if (!c) return st;
+        YAS_TRY_CUDA(cudaGraphLaunch(c->exec, b->stream));
+        b->last_kernels = c->kernels;
+    } else {
+        b->last_kernels = 0;
+    }
+    YAS_TRY_CUDA(cudaEventRecord(b->ev_end, b->stream));
+    for (size_t i = 0; i < key.size(); ++i) {
+        if (key[i] == kFirst) session_finish_first(b->s[i]);
+        else if (key[i] != kIdle) session_finish_tracked(b->s[i]);
+    }
+    b->last_key = key;
+    b->pending = true;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_wait(yas_batch *b, yas_pose *out_Tcm, int *out_status, float *out_ms) {
+    if (!b) return YAS_ERR_BAD_ARG;
+    if (!b->pending) return YAS_ERR_STATE;
+    YAS_TRY_CUDA(cudaEventSynchronize(b->ev_end));
+    if (out_ms) YAS_TRY_CUDA(cudaEventElapsedTime(out_ms, b->ev_start, b->ev_end));
+    for (size_t i = 0; i < b->last_key.size(); ++i) {
+        if (b->last_key[i] == kIdle) continue;
+        session_result(b->s[i], out_Tcm ? out_Tcm + i : nullptr, out_status ? out_status + i : nullptr);
+    }
+    b->pending = false;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_kernels_per_step(yas_batch *b, int *out) {
+    if (!b || !out) return YAS_ERR_BAD_ARG;
+    *out = b->last_kernels;
+    return YAS_OK;
+}
+
+YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const uint16_t *const *depth, int frames,
+                               int on_device, yas_batch_tuning *out) {
+    if (!b || !rgb || !depth || frames < 3) return YAS_ERR_BAD_ARG;
+    const size_t n = b->s.size();
+    for (size_t i = 0; i < n; ++i)
+        if (!rgb[i] || !depth[i]) return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    // scratch copies of the sessions, stepped by a scratch batch
+    std::vector<yas_session *> clones(n, nullptr);
+    yas_batch *cb = nullptr;
+    int st = YAS_OK;
+    for (size_t i = 0; i < n && st == YAS_OK; ++i) {
+        yas_session_config cfg = session_config(b->s[i]);
+        st = yas_session_create(&clones[i], &cfg, nullptr);
+    }
+    if (st == YAS_OK) st = yas_batch_create(&cb, clones.data(), (int)n, nullptr);
+    std::vector<const uint8_t *> fr(n);
+    std::vector<const uint16_t *> fd(n);
+    std::vector<float> ms;
+    // median device time of one pass over the calibration frames (tracked steps)
+    auto measure = [&](const yas_batch_tuning &t, float *median) -> int {
+        YAS_TRY(yas_batch_set_tuning(cb, &t));
+        for (yas_session *c : clones) YAS_TRY(session_restart(c));
+        ms.clear();
+        for (int f = 0; f < frames; ++f) {
+            for (size_t i = 0; i < n; ++i) {
+                const yas_session_config &c = session_config(clones[i]);
+                const size_t px = (size_t)c.width * c.height;
+                fr[i] = rgb[i] + (size_t)f * px * 3;
+                fd[i] = depth[i] + (size_t)f * px;
+            }
+            YAS_TRY(yas_batch_step(cb, fr.data(), fd.data(), nullptr, on_device));
+            float t_ms = 0.0f;
+            YAS_TRY(yas_batch_wait(cb, nullptr, nullptr, &t_ms));
+            if (f > 0) ms.push_back(t_ms);
+        }
+        std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
+        *median = ms[ms.size() / 2];
+        return YAS_OK;
+    };
+    yas_batch_tuning best = b->tuning;
+    float best_ms = 0.0f;
+    if (st == YAS_OK) st = measure(best, &best_ms);
+    // coordinate descent, one pass: GN share, march CTA shape, integration grid
+    const int gn_c[3] = {16384, 32768, 65536};
+    const int mw_c[3] = {1, 2, 4};
+    const int ig_c[3] = {152 * 4, 152 * 8, 152 * 16};
+    for (int knob = 0; knob < 3 && st == YAS_OK; ++knob) {
+        for (int v = 0; v < 3 && st == YAS_OK; ++v) {
+            yas_batch_tuning t = best;
+            int *field = knob == 0 ? &t.gn_pixels_per_cta : (knob == 1 ? &t.march_warps_x : &t.integrate_ctas);
+            const int value = knob == 0 ? gn_c[v] : (knob == 1 ? mw_c[v] : ig_c[v]);
+            if (*field == value) continue;
+            *field = value;
+            float m = 0.0f;
+            st = measure(t, &m);
+            if (st == YAS_OK && m < best_ms) {
+                best_ms = m;
+                best = t;
+            }
+        }
+    }
+    if (cb) yas_batch_destroy(cb);
+    for (yas_session *c : clones)
+        if (c) yas_session_destroy(c);
+    if (st != YAS_OK) return st;
+    apply_tuning(b, best);
+    if (out) *out = best;
+    return YAS_OK;
+}
+
+}  // extern "C"

@@ -299,8 +299,8 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
 
 template <int SIGN>
 static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                                  const PosePair *P, const int *skip, cudaStream_t s) {
-    const int grid = 152 * 8;
+                                  const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0) {
+    const int grid = grid_ctas > 0 ? grid_ctas : 152 * 8;
     switch (fmt) {
         case YAS_VOXEL_F32:
             integrate_kernel<YAS_VOXEL_F32, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
@@ -315,8 +315,8 @@ static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, 
 }
 
 void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                      const PosePair *P, const int *skip, cudaStream_t s) {
-    launch_integrate_sign<1>(m, fmt, depth, pitch_elems, cam, P, skip, s);
+                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas) {
+    launch_integrate_sign<1>(m, fmt, depth, pitch_elems, cam, P, skip, s, grid_ctas);
 }
 
 void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,

@@ -297,16 +297,17 @@ __device__ __forceinline__ float4 ray_finish(VoxelReader<FMT> &rd, float rstep, 
     return out;
 }
 
-// One thread per pixel; a CTA covers 16x8 pixels, each warp a compact 8x4
-// tile, so its rays travel similar depths.
-template <int FMT>
+// One thread per pixel; each warp a compact 8x4 tile, so its rays travel
+// similar depths; the CTA's four warp tiles lie WX across and 4/WX down
+// (a CTA covers 8WX x 16/WX pixels).
+template <int FMT, int WX>
 __global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const PosePair *P,
                                                     const float *__restrict__ znear,
                                                     const float *__restrict__ zfar, int zw, float4 *vmap,
                                                     int vpitch, const int *skip) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    const int x = blockIdx.x * (8 * WX) + (warp % WX) * 8 + (lane & 7);
+    const int y = blockIdx.y * (16 / WX) + (warp / WX) * 4 + (lane >> 3);
     if (x >= cam.w || y >= cam.h) return;
     float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
                              -1.0f);
@@ -325,23 +326,34 @@ __global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const Pos
     vmap[(size_t)y * vpitch + x] = out;
 }
 
-void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
+template <int WX>
+static void launch_march_wx(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
                             float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
-    dim3 grid((cam.w + 15) / 16, (cam.h + 7) / 8);
+    dim3 grid((cam.w + 8 * WX - 1) / (8 * WX), (cam.h + 16 / WX - 1) / (16 / WX));
     switch (fmt) {
         case YAS_VOXEL_F32:
-            march_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                             vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_F32, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                 vmap_pitch_elems, skip);
             break;
         case YAS_VOXEL_F16:
-            march_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                             vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_F16, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                 vmap_pitch_elems, skip);
             break;
         default:
-            march_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                             vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_S24, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                 vmap_pitch_elems, skip);
             break;
     }
+}
+
+void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
+                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int warps_x) {
+    if (warps_x == 1)
+        launch_march_wx<1>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
+    else if (warps_x == 4)
+        launch_march_wx<4>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
+    else
+        launch_march_wx<2>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
 }
 
 __global__ void vmap_to_depth_kernel(const float4 *vmap, int vpitch, float *depth, int dpitch, int w,

@@ -146,6 +146,7 @@ struct yas_session {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int kernels_per_frame = 0;
+    LaunchShape shape;
     Cam cam;
     // profiling: events recorded between launches of an eager frame
     std::vector<cudaEvent_t> prof_events;
@@ -176,7 +177,8 @@ static void enqueue_fusion(yas_session *s, const int *skip) {
     prof_mark(s, kStVisible);
     launch_visible(v, s->cam, &s->fs->pp, skip, s->stream);
     prof_mark(s, kStIntegrate);
-    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream);
+    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream,
+                     s->shape.integrate_ctas);
 }
 
 static void enqueue_first_frame(yas_session *s) {
@@ -198,7 +200,7 @@ static void enqueue_raycast_branch(yas_session *s, cudaStream_t st) {
     launch_zrange(v, s->rc->cam, &s->fs->pp, s->rc->rb, nullptr, st);
     prof_mark(s, kStMarch);
     launch_march(v, s->map->cfg.voxel_format, s->rc->cam, &s->fs->pp, s->rc->rb, tr->refb(0).vmap, s->cfg.width,
-                 nullptr, st);
+                 nullptr, st, s->shape.march_warps_x);
     prof_mark(s, kStModel);
     tracker_model(tr, st);
 }
@@ -307,6 +309,16 @@ int session_copy_input(yas_session *s, const uint8_t *rgb, const uint16_t *depth
 
 bool session_needs_init(const yas_session *s) { return s->frames == 0; }
 
+static void drop_graphs(yas_session *s) {
+    for (int i = 0; i < 2; ++i) {
+        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
+        s->exec[i] = s->pre_exec[i] = nullptr;
+    }
+    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
+    s->post_exec = nullptr;
+}
+
 // Drops captured graphs that name map arrays which have since moved; a
 // hibernated map cannot run frames.
 static int check_graphs(yas_session *s) {
@@ -315,13 +327,7 @@ static int check_graphs(yas_session *s) {
     bool same = true;
     for (int i = 0; i < 5; ++i) same = same && now[i] == s->graph_arrays[i];
     if (same) return YAS_OK;
-    for (int i = 0; i < 2; ++i) {
-        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
-        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
-        s->exec[i] = s->pre_exec[i] = nullptr;
-    }
-    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
-    s->post_exec = nullptr;
+    drop_graphs(s);
     for (int i = 0; i < 5; ++i) s->graph_arrays[i] = now[i];
     return YAS_OK;
 }
@@ -353,6 +359,33 @@ int session_launch_post(yas_session *s) {
 
 yas_tracker *session_tracker(yas_session *s) { return s->tr; }
 cudaStream_t session_stream(yas_session *s) { return s->stream; }
+yas_map *session_map_handle(yas_session *s) { return s->map; }
+const yas_session_config &session_config(const yas_session *s) { return s->cfg; }
+
+void session_set_shape(yas_session *s, const LaunchShape &shape) {
+    s->shape = shape;
+    drop_graphs(s);
+}
+
+const LaunchShape &session_shape(const yas_session *s) { return s->shape; }
+
+void session_enqueue_first(yas_session *s) { enqueue_first_frame(s); }
+void session_enqueue_pre(yas_session *s) { enqueue_pre(s); }
+void session_enqueue_post(yas_session *s) { enqueue_post(s); }
+
+void session_finish_first(yas_session *s) { s->frames++; }
+
+void session_finish_tracked(yas_session *s) {
+    s->tr->cur = 1 - s->tr->cur;
+    s->frames++;
+}
+
+int session_restart(yas_session *s) {
+    YAS_TRY_CUDA(cudaStreamSynchronize(s->stream));
+    YAS_TRY(yas_map_reset(s->map));
+    s->frames = 0;
+    return YAS_OK;
+}
 
 void session_result(const yas_session *s, yas_pose *Tcm, int *status) {
     if (Tcm)

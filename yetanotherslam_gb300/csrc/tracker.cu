@@ -1050,14 +1050,15 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
 // A tracker takes a fixed number of CTAs in a batch, set by its resolution
 // alone (one per 32 Ki level-0 pixels, 1..16), so its result does not depend
 // on the rest of the batch.
-int gn_batch_ctas(const yas_tracker *tr) {
+int gn_batch_ctas(const yas_tracker *tr, int pixels_per_cta) {
     const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
-    return (int)std::min<long long>(16, std::max<long long>(1, (P0 + 32767) / 32768));
+    const long long q = std::max(1024, pixels_per_cta);
+    return (int)std::min<long long>(16, std::max<long long>(1, (P0 + q - 1) / q));
 }
 
-void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out) {
+void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out, int pixels_per_cta) {
     memset(out, 0, sizeof(*out));
-    out->nctas = gn_batch_ctas(tr);
+    out->nctas = gn_batch_ctas(tr, pixels_per_cta);
     out->cta0 = cta0;
     fill_levels(tr, out->nctas, out->lv);
     out->L = tr->L;

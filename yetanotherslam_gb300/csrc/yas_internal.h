@@ -71,8 +71,9 @@ void launch_allocate(const MapDev &m, int fmt, const float *depth, int pitch_ele
 void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const int *skip,
                     cudaStream_t s);
 // Integrates depth into the visible blocks.
+// `grid_ctas` 0: the default grid (152 x 8 CTAs of 256 threads).
 void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                      const PosePair *P, const int *skip, cudaStream_t s);
+                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0);
 void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
                         const PosePair *P, cudaStream_t s);
 // Submap fusion and growth (fusion.cu)
@@ -96,8 +97,10 @@ struct RaycastBuffers {
 };
 void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
                    const int *skip, cudaStream_t s);
+// `warps_x`: a 128-thread CTA's four 8x4-pixel warp tiles side by side in x
+// (1: 8x16 pixels, 2: 16x8, the default, 4: 32x4); the output is the same.
 void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
-                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s);
+                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int warps_x = 2);
 void launch_vmap_to_depth(const float4 *vmap, int vpitch, float *depth, int dpitch, int w, int h,
                           cudaStream_t s);
 

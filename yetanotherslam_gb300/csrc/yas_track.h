@@ -149,8 +149,10 @@ void tracker_depth(yas_tracker *tr, const void *src, int is_u16, int pitch, floa
                    bool reference, cudaStream_t s);
 void tracker_model(yas_tracker *tr, cudaStream_t s);  // model pyramid from ref vmap[0]
 // Batched Gauss-Newton (many trackers, one cooperative launch):
-int gn_batch_ctas(const yas_tracker *tr);               // CTAs a tracker takes in a batch
-void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out);  // descriptor of its current frame
+// CTAs a tracker takes in a batch: one per `pixels_per_cta` level-0 pixels, 1..16
+int gn_batch_ctas(const yas_tracker *tr, int pixels_per_cta = 32768);
+// descriptor of its current frame
+void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out, int pixels_per_cta = 32768);
 int gn_batch_capacity();                                // co-resident CTAs of the batched launch
 cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *dev_cta_item, int grid,
                             cudaStream_t s);
