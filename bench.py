@@ -250,6 +250,7 @@ def run_gpu(args):
     # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
     cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
     served = run_served(100 + 1000 * rank) if args.served else None
+    batched = run_batched(7 + 1000 * rank) if args.batched else None
 
     value = world * args.steps / (total_ms * 1e-3)
     line = {
@@ -280,6 +281,7 @@ def run_gpu(args):
                      "traffic": traffic},
         "cpu_baseline": cpu,
         "served": served,
+        "batched": batched,
         "clocks": clk.summary(),
     }
     if rank == 0:
@@ -409,6 +411,110 @@ def run_served(seed: int = 100):
             "served_over_plain": round(sat["fps"] / plain_fps, 2)}
 
 
+BATCHED = {"submaps": 16, "resolutions": [[320, 240], [480, 360], [640, 480]], "voxel_m": [0.005, 0.008],
+           "frames": [5, 60], "hash_slots": 1 << 20, "max_blocks": 1 << 17, "tsdf": "fp16+u16",
+           "calibration_frames": 4}
+
+
+def run_batched(seed: int = 7):
+    """C3: 16 keyframe submaps of uneven size (a seeded mix of 320x240 / 480x360 / 640x480, 5 or 8 mm
+    voxels, 5-60 frames each), inputs resident in HBM, stepped by yas_batch (one graph launch per step,
+    one batched GN launch) with autotuned launch shapes; against the same submaps run one after the
+    other through the single-session graph path, and through the plain FP32 per-frame form."""
+    import torch
+
+    from yetanotherslam_gb300 import batching
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import synth
+
+    cfg = BATCHED
+    rng = np.random.default_rng(seed)
+    plan = []
+    for i in range(cfg["submaps"]):
+        W, H = cfg["resolutions"][int(rng.integers(len(cfg["resolutions"])))]
+        vs = float(cfg["voxel_m"][int(rng.integers(len(cfg["voxel_m"])))])
+        n = int(rng.integers(cfg["frames"][0], cfg["frames"][1] + 1))
+        fr = make_frames(max(n, cfg["calibration_frames"]), W, H, seed * 100 + i)
+        dev = [(torch.from_numpy(f.rgb).cuda(), torch.from_numpy(f.depth.view(np.int16)).cuda()) for f in fr]
+        plan.append((W, H, vs, n, fr, dev))
+    torch.cuda.synchronize()
+
+    def sessions(fmt=rf.VOXEL_F16, **kw):
+        return [rf.Session(W, H, synth.intrinsics(W, H), hash_slots=cfg["hash_slots"], max_blocks=cfg["max_blocks"],
+                           voxel_size=vs, voxel_format=fmt, num_levels=3, iterations=(10, 5, 3), **kw)
+                for W, H, vs, _, _, _ in plan]
+
+    def run_batch(tuning):
+        ss = sessions()
+        b = batching.Batch(ss)
+        if tuning is not None:
+            b.tuning = tuning
+        steps = max(p[3] for p in plan)
+        total_ms, frames, bad = 0.0, 0, 0
+        t0 = time.perf_counter()
+        for f in range(steps):
+            b.step([p[5][f] if f < p[3] else None for p in plan])
+            _, st, ms = b.wait()
+            total_ms += ms
+            frames += int((st >= 0).sum())
+            bad += int((st > 0).sum())
+        wall = time.perf_counter() - t0
+        kernels = b.kernels_per_step()
+        b.close()
+        for s in ss:
+            s.close()
+        return frames, total_ms, wall, bad, kernels
+
+    # autotune on scratch copies, from each submap's first frames
+    ss = sessions()
+    b = batching.Batch(ss)
+    k = cfg["calibration_frames"]
+    calib = [(torch.stack([d[0] for d in p[5][:k]]), torch.stack([d[1] for d in p[5][:k]])) for p in plan]
+    t0 = time.perf_counter()
+    tuned = b.autotune(calib)
+    tune_s = time.perf_counter() - t0
+    b.close()
+    for s in ss:
+        s.close()
+    run_batch(None)  # graph captures and allocator warm-up
+    f_def, ms_def, wall_def, bad_def, _ = run_batch(None)
+    f_tun, ms_tun, wall_tun, bad_tun, kernels = run_batch(tuned)
+
+    def one_at_a_time(fmt, **kw):
+        ss = sessions(fmt, **kw)
+        for s, p in zip(ss, plan):  # warm-up: graph capture of both parities
+            for f in range(3):
+                s.process(*p[5][f])
+        for s in ss:
+            s.close()
+        ss = sessions(fmt, **kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n = 0
+        for s, p in zip(ss, plan):
+            for f in range(p[3]):
+                s.process(*p[5][f])
+                n += 1
+        wall = time.perf_counter() - t0
+        for s in ss:
+            s.close()
+        return n / wall
+
+    seq_fps = one_at_a_time(rf.VOXEL_F16)
+    plain_fps = one_at_a_time(rf.VOXEL_F32, use_graph=False, fused_schedule=False)
+    t_fps = f_tun / (ms_tun * 1e-3)
+    return {"config": dict(cfg, mix=[{"res": f"{p[0]}x{p[1]}", "voxel_m": p[2], "frames": p[3]} for p in plan]),
+            "submap_frames": f_tun, "steps": max(p[3] for p in plan), "kernels_per_step": kernels,
+            "tuning": {"march_warps_x": tuned.march_warps_x, "integrate_ctas": tuned.integrate_ctas,
+                       "gn_pixels_per_cta": tuned.gn_pixels_per_cta}, "autotune_s": round(tune_s, 2),
+            "batched_fps_device": round(t_fps, 1), "batched_fps_wall": round(f_tun / wall_tun, 1),
+            "batched_default_fps_device": round(f_def / (ms_def * 1e-3), 1),
+            "frame_status_nonzero": bad_tun + bad_def,
+            "one_session_at_a_time_fps": round(seq_fps, 1), "plain_fp32_per_frame_fps": round(plain_fps, 1),
+            "batched_over_one_at_a_time": round(t_fps / seq_fps, 2),
+            "batched_over_plain": round(t_fps / plain_fps, 2)}
+
+
 def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
     import oracle
 
@@ -475,6 +581,7 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=4)
     ap.add_argument("--cpu-frames", type=int, default=8)
     ap.add_argument("--served", type=int, default=1, help="1: also measure 32 served sessions (C4)")
+    ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

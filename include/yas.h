@@ -402,14 +402,18 @@ YAS_API int yas_session_profile_frame(yas_session *s, const uint8_t *rgb, const 
 typedef struct yas_batch yas_batch;
 
 typedef struct yas_batch_tuning {
-    int march_warps_x;     /* ray-march CTA shape: 1 (8x16 px), 2 (16x8), 4 (32x4)     */
+    int march_warps_x;     /* ray march: 1, 2, 4: one thread per pixel, CTA tiles of
+                            * 8x16, 16x8, 32x4 pixels; 0: persistent warps taking 8x4
+                            * tiles from a queue (the vertex map is the same for all) */
     int integrate_ctas;    /* CTAs of the integration grid, 256 threads each          */
-    int gn_pixels_per_cta; /* batched GN: one 1024-thread CTA per this many level-0
-                            * pixels (1..16 CTAs per session); fixes each session's
-                            * summation order, so results depend on it, not on the mix */
+    int gn_pixels_per_cta; /* batched GN: 0 splits the co-resident 1024-thread CTAs
+                            * over the step's sessions in proportion to their pixels;
+                            * > 0: one CTA per this many level-0 pixels (1..16 per
+                            * session), which fixes each session's summation order, so
+                            * its results do not depend on the rest of the batch      */
 } yas_batch_tuning;
 
-/* Defaults: 2, 1216 (152 x 8), 32768. */
+/* Defaults: 2, 1216 (152 x 8), 0. */
 YAS_API int yas_batch_tuning_default(yas_batch_tuning *t);
 YAS_API int yas_batch_create(yas_batch **out, yas_session *const *sessions, int count, void *stream);
 YAS_API int yas_batch_destroy(yas_batch *b);

@@ -40,7 +40,7 @@ struct CachedStep {
 };
 
 struct GNGroup {
-    int item0, nitems, cta0, nctas;
+    int item0, nitems, cta0, nctas, pix;
 };
 
 constexpr size_t kMaxCached = 8;
@@ -71,8 +71,9 @@ static LaunchShape shape_of(const yas_batch_tuning &t) {
 }
 
 static bool tuning_valid(const yas_batch_tuning &t) {
-    return (t.march_warps_x == 1 || t.march_warps_x == 2 || t.march_warps_x == 4) && t.integrate_ctas > 0 &&
-           t.integrate_ctas <= (1 << 20) && t.gn_pixels_per_cta >= 1024;
+    return (t.march_warps_x == 0 || t.march_warps_x == 1 || t.march_warps_x == 2 || t.march_warps_x == 4) &&
+           t.integrate_ctas > 0 &&
+           t.integrate_ctas <= (1 << 20) && (t.gn_pixels_per_cta == 0 || t.gn_pixels_per_cta >= 1024);
 }
 
 static void free_cached(CachedStep &c) {
@@ -131,30 +132,84 @@ static int count_kernels(cudaGraph_t g, int *out) {
     return YAS_OK;
 }
 
-// The GN descriptors of the tracked sessions, packed into cooperative launches
-// of at most `capacity` CTAs each (a session never straddles two).
+// The GN descriptors of the tracked sessions, in cooperative launches of at
+// most `capacity` CTAs each (a session never straddles two).
+//   gn_pixels_per_cta > 0: every session takes a fixed share set by its
+//     resolution alone, so its result does not depend on the rest of the
+//     batch; sessions are packed greedily.
+//   gn_pixels_per_cta == 0: the co-resident CTAs are split over the sessions
+//     in proportion to their level-0 pixels (at least one each), so one
+//     launch keeps every SM busy and a lone session gets the whole GPU.
 static int plan_gn(yas_batch *b, const std::vector<uint8_t> &key, std::vector<GNBatchItem> &items,
                    std::vector<unsigned short> &cta_item, std::vector<GNGroup> &groups) {
     const int capacity = gn_batch_capacity();
     if (capacity <= 0) return YAS_ERR_STATE;  // no cooperative launch on this device
-    GNGroup g = {0, 0, 0, 0};
-    for (size_t i = 0; i < b->s.size(); ++i) {
-        if (key[i] < kTrack0) continue;
-        yas_tracker *tr = session_tracker(b->s[i]);
-        const int n = gn_batch_ctas(tr, b->tuning.gn_pixels_per_cta);
-        if (n > capacity) return YAS_ERR_CAPACITY;
-        if (g.nctas + n > capacity) {
-            groups.push_back(g);
-            g = {(int)items.size(), 0, (int)cta_item.size(), 0};
-        }
+    std::vector<yas_tracker *> tracked;
+    for (size_t i = 0; i < b->s.size(); ++i)
+        if (key[i] >= kTrack0) tracked.push_back(session_tracker(b->s[i]));
+    auto close_group = [&](GNGroup &g) {
+        if (!g.nitems) return;
+        g.pix = gn_batch_pix(items.data() + g.item0, g.nitems);
+        groups.push_back(g);
+    };
+    auto add = [&](GNGroup &g, yas_tracker *tr, int n) {
         GNBatchItem it;
-        gn_batch_item(tr, g.nctas, &it, b->tuning.gn_pixels_per_cta);
+        gn_batch_item_ctas(tr, g.nctas, n, &it);
         for (int c = 0; c < it.nctas; ++c) cta_item.push_back((unsigned short)g.nitems);
         items.push_back(it);
         g.nitems += 1;
         g.nctas += it.nctas;
+    };
+    const int ppc = b->tuning.gn_pixels_per_cta;
+    if (ppc > 0) {
+        GNGroup g = {0, 0, 0, 0, 0};
+        for (yas_tracker *tr : tracked) {
+            const int n = gn_batch_ctas(tr, ppc);
+            if (n > capacity) return YAS_ERR_CAPACITY;
+            if (g.nctas + n > capacity) {
+                close_group(g);
+                g = {(int)items.size(), 0, (int)cta_item.size(), 0, 0};
+            }
+            add(g, tr, n);
+        }
+        close_group(g);
+        return YAS_OK;
     }
-    if (g.nitems) groups.push_back(g);
+    for (size_t g0 = 0; g0 < tracked.size(); g0 += (size_t)capacity) {
+        const size_t g1 = std::min(tracked.size(), g0 + (size_t)capacity);
+        const size_t m = g1 - g0;
+        std::vector<double> q(m);
+        std::vector<int> n(m);
+        double total = 0.0;
+        for (size_t k = 0; k < m; ++k) {
+            const yas_tracker *tr = tracked[g0 + k];
+            q[k] = (double)tr->cam[0].w * tr->cam[0].h;
+            total += q[k];
+        }
+        int sum = 0;
+        for (size_t k = 0; k < m; ++k) {
+            q[k] = q[k] * capacity / total;
+            n[k] = std::max(1, (int)q[k]);
+            sum += n[k];
+        }
+        while (sum > capacity) {  // the at-least-one rule overshot: take from the largest
+            size_t big = 0;
+            for (size_t k = 1; k < m; ++k)
+                if (n[k] > n[big]) big = k;
+            --n[big];
+            --sum;
+        }
+        while (sum < capacity) {  // leftovers to the largest remainders
+            size_t best = 0;
+            for (size_t k = 1; k < m; ++k)
+                if (q[k] - n[k] > q[best] - n[best]) best = k;
+            ++n[best];
+            ++sum;
+        }
+        GNGroup g = {(int)items.size(), 0, (int)cta_item.size(), 0, 0};
+        for (size_t k = 0; k < m; ++k) add(g, tracked[g0 + k], n[k]);
+        close_group(g);
+    }
     return YAS_OK;
 }
 
@@ -194,7 +249,7 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
         if (key[i] >= kTrack0) err = cudaStreamWaitEvent(b->stream, b->ev_pre[i], 0);
     for (const GNGroup &g : groups) {
         if (err != cudaSuccess) break;
-        err = launch_gn_batch(out.d_items + g.item0, out.d_map + g.cta0, g.nctas, b->stream);
+        err = launch_gn_batch(out.d_items + g.item0, out.d_map + g.cta0, g.nctas, b->stream, g.pix);
     }
     if (err == cudaSuccess && !groups.empty()) err = cudaEventRecord(b->ev_gn, b->stream);
     for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
@@ -263,7 +318,7 @@ YAS_API int yas_batch_tuning_default(yas_batch_tuning *t) {
     if (!t) return YAS_ERR_BAD_ARG;
     t->march_warps_x = 2;
     t->integrate_ctas = 152 * 8;
-    t->gn_pixels_per_cta = 32768;
+    t->gn_pixels_per_cta = 0;
     return YAS_OK;
 }
 
@@ -438,11 +493,11 @@ YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const ui
     float best_ms = 0.0f;
     if (st == YAS_OK) st = measure(best, &best_ms);
     // coordinate descent, one pass: GN share, march CTA shape, integration grid
-    const int gn_c[3] = {16384, 32768, 65536};
-    const int mw_c[3] = {1, 2, 4};
-    const int ig_c[3] = {152 * 4, 152 * 8, 152 * 16};
+    const int gn_c[4] = {0, 16384, 32768, 65536};
+    const int mw_c[4] = {0, 1, 2, 4};
+    const int ig_c[4] = {152 * 4, 152 * 8, 152 * 16, 152 * 8};
     for (int knob = 0; knob < 3 && st == YAS_OK; ++knob) {
-        for (int v = 0; v < 3 && st == YAS_OK; ++v) {
+        for (int v = 0; v < 4 && st == YAS_OK; ++v) {
             yas_batch_tuning t = best;
             int *field = knob == 0 ? &t.gn_pixels_per_cta : (knob == 1 ? &t.march_warps_x : &t.integrate_ctas);
             const int value = knob == 0 ? gn_c[v] : (knob == 1 ? mw_c[v] : ig_c[v]);

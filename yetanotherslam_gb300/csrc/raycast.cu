@@ -20,18 +20,22 @@
 // Deliberate differences: a missed ray writes w = -1 (the reference leaves w
 // stale on its early return, RayTraceEngine.cu:338-347); the 8 trilinear
 // corners are floor(p) + {0,1}^3 (the reference floors p + offset per corner).
+#include <algorithm>
 #include <cfloat>
 
 #include "yas_internal.h"
 
 namespace yas {
 
-__global__ void zrange_reset_kernel(float *znear, float *zfar, int n, unsigned *n_render) {
+__global__ void zrange_reset_kernel(float *znear, float *zfar, int n, unsigned *n_render, unsigned *queue) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         znear[i] = 100.0f;
         zfar[i] = 0.0f;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *n_render = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *n_render = 0;
+        *queue = 0u;
+    }
 }
 
 __device__ __forceinline__ int clamp_floor(float v) {
@@ -91,7 +95,7 @@ __global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, con
 void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
                    const int *skip, cudaStream_t s) {
     int n = rb.zw * rb.zh;
-    zrange_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render);
+    zrange_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render, rb.queue);
     zrange_fill_kernel<<<152 * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip);
 }
 
@@ -326,6 +330,112 @@ __global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const Pos
     vmap[(size_t)y * vpitch + x] = out;
 }
 
+// Persistent march: resident warps take 8x4-pixel tiles from a queue (one
+// atomic per tile on rb.queue, tiles row-major), a warp taking the next tile
+// once all its rays are done, so no SM idles behind a partial last wave.
+// Each ray runs exactly the steps of march_kernel, so the vertex map is the
+// same bit for bit.
+template <int FMT>
+__global__ void __launch_bounds__(128) march_persistent_kernel(MapDev m, Cam cam, const PosePair *P,
+                                                               const float *__restrict__ znear,
+                                                               const float *__restrict__ zfar, int zw, float4 *vmap,
+                                                               int vpitch, const int *skip, unsigned *queue,
+                                                               unsigned total) {
+    const unsigned lane = lane_id();
+    const int tiles_x = (cam.w + 7) >> 3;
+    const float4 miss = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                                    __int_as_float(0x7fffffff), -1.0f);
+    if (skip && *skip) {
+        for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+            const int t = (int)(p >> 5), l = (int)(p & 31u);
+            const int x = (t % tiles_x) * 8 + (l & 7), y = (t / tiles_x) * 4 + (l >> 3);
+            if (x < cam.w && y < cam.h) vmap[(size_t)y * vpitch + x] = miss;
+        }
+        return;
+    }
+    const float vsinv = 1.0f / m.voxel_size;
+    const float rstep = m.trunc / m.voxel_size;
+    VoxelReader<FMT> rd(m);
+    RayState R;
+    bool active = false, drained = false;
+    int x = 0, y = 0;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!drained && idle == 0xffffffffu) {
+            const int leader = __ffs(idle) - 1;
+            unsigned base = 0u;
+            if ((int)lane == leader) base = atomicAdd(queue, (unsigned)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + (unsigned)__popc(idle) >= total) drained = true;
+            if (!active) {
+                const unsigned p = base + (unsigned)__popc(idle & ((1u << lane) - 1u));
+                if (p < total) {
+                    const int t = (int)(p >> 5), l = (int)(p & 31u);
+                    x = (t % tiles_x) * 8 + (l & 7);
+                    y = (t / tiles_x) * 4 + (l >> 3);
+                    if (x < cam.w && y < cam.h) {
+                        if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)),
+                                      __ldg(zfar + (y >> 3) * zw + (x >> 3)), x, y, R))
+                            active = true;
+                        else
+                            vmap[(size_t)y * vpitch + x] = miss;
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (drained) break;
+            continue;
+        }
+        if (active && ray_step(rd, rstep, R)) {
+            vmap[(size_t)y * vpitch + x] = ray_finish(rd, rstep, vsinv, P->Tinv, R);
+            active = false;
+        }
+    }
+}
+
+static int march_resident_ctas(int fmt) {
+    static int cache[3][64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || fmt < 0 || fmt > 2) return 152;
+    int &c = cache[fmt][dev];
+    if (c == 0) {
+        int sms = 0, nb = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (fmt == YAS_VOXEL_F32)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_F32>, 128, 0);
+        else if (fmt == YAS_VOXEL_F16)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_F16>, 128, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_S24>, 128, 0);
+        cudaGetLastError();
+        c = std::max(1, nb) * std::max(1, sms);
+    }
+    return c;
+}
+
+static void launch_march_persistent(const MapDev &m, int fmt, const Cam &cam, const PosePair *P,
+                                    const RaycastBuffers &rb, float4 *vmap, int vmap_pitch_elems, const int *skip,
+                                    cudaStream_t s) {
+    const unsigned total = (unsigned)(((cam.w + 7) / 8) * ((cam.h + 3) / 4) * 32);
+    const int grid = std::min(march_resident_ctas(fmt), (int)((total + 127) / 128));
+    switch (fmt) {
+        case YAS_VOXEL_F32:
+            march_persistent_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                        vmap_pitch_elems, skip, rb.queue, total);
+            break;
+        case YAS_VOXEL_F16:
+            march_persistent_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                        vmap_pitch_elems, skip, rb.queue, total);
+            break;
+        default:
+            march_persistent_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                        vmap_pitch_elems, skip, rb.queue, total);
+            break;
+    }
+}
+
 template <int WX>
 static void launch_march_wx(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
                             float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
@@ -348,7 +458,9 @@ static void launch_march_wx(const MapDev &m, int fmt, const Cam &cam, const Pose
 
 void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
                   float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int warps_x) {
-    if (warps_x == 1)
+    if (warps_x == 0)
+        launch_march_persistent(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
+    else if (warps_x == 1)
         launch_march_wx<1>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
     else if (warps_x == 4)
         launch_march_wx<4>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);

@@ -188,7 +188,8 @@ int dispatch_gn(yas_server *srv, const std::vector<ServedSession *> &batch) {
                                  cudaMemcpyHostToDevice, srv->gn_stream));
     YAS_TRY_CUDA(cudaMemcpyAsync(srv->d_map[k], srv->h_map[k], (size_t)cta0 * sizeof(unsigned short),
                                  cudaMemcpyHostToDevice, srv->gn_stream));
-    YAS_TRY_CUDA(launch_gn_batch(srv->d_items[k], srv->d_map[k], cta0, srv->gn_stream));
+    YAS_TRY_CUDA(launch_gn_batch(srv->d_items[k], srv->d_map[k], cta0, srv->gn_stream,
+                                 gn_batch_pix(srv->h_items[k], (int)batch.size())));
     YAS_TRY_CUDA(cudaEventRecord(srv->gn_done[k], srv->gn_stream));
     for (ServedSession *ss : batch) {
         cudaStream_t st = session_stream(ss->s);

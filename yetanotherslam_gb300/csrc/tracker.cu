@@ -884,11 +884,14 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_consta
 // Fused schedules of a batch of trackers in one launch: CTA b runs for item
 // cta_item[b] as its CTA b - cta0 of nctas.  Items never wait on each other,
 // so an item's result is the same alone and in any batch.
+// PIX > 0: every item's CTAs own at most PIX pixels per thread on every level
+// (residuals kept in registers); PIX == 0: any share (residuals in res4).
+template <int PIX>
 __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused_batch(const GNBatchItem *__restrict__ items,
                                                                     const unsigned short *__restrict__ cta_item) {
     const GNBatchItem &it = items[cta_item[blockIdx.x]];
-    gn_schedule<0>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st, blockIdx.x - (unsigned)it.cta0,
-                   (unsigned)it.nctas);
+    gn_schedule<PIX>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st,
+                     blockIdx.x - (unsigned)it.cta0, (unsigned)it.nctas);
 }
 
 // ---------------------------------------------------------------- host side
@@ -1057,8 +1060,12 @@ int gn_batch_ctas(const yas_tracker *tr, int pixels_per_cta) {
 }
 
 void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out, int pixels_per_cta) {
+    gn_batch_item_ctas(tr, cta0, gn_batch_ctas(tr, pixels_per_cta), out);
+}
+
+void gn_batch_item_ctas(yas_tracker *tr, int cta0, int nctas, GNBatchItem *out) {
     memset(out, 0, sizeof(*out));
-    out->nctas = gn_batch_ctas(tr, pixels_per_cta);
+    out->nctas = std::max(1, std::min(nctas, kFusedMaxCtas));
     out->cta0 = cta0;
     fill_levels(tr, out->nctas, out->lv);
     out->L = tr->L;
@@ -1079,15 +1086,26 @@ int gn_batch_capacity() {
         int sms = 0, nb = 0, coop = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gn_fused_batch, kFusedThreads, 0);
+        int lowest = 1 << 30;
+        for (auto k : {gn_fused_batch<0>, gn_fused_batch<1>, gn_fused_batch<2>, gn_fused_batch<4>}) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kFusedThreads, 0);
+            lowest = std::min(lowest, nb);
+        }
         cudaGetLastError();
-        cap[dev] = coop ? std::max(0, nb * sms) : -1;
+        cap[dev] = coop ? std::max(0, std::min(lowest * sms, kFusedMaxCtas)) : -1;
     }
     return cap[dev];
 }
 
+int gn_batch_pix(const GNBatchItem *items, int n) {
+    int pix = 0;
+    for (int i = 0; i < n; ++i)
+        for (int l = 0; l < items[i].L; ++l) pix = std::max(pix, items[i].lv[l].pix);
+    return pix <= 1 ? 1 : (pix <= 2 ? 2 : (pix <= 4 ? 4 : 0));
+}
+
 cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *dev_cta_item, int grid,
-                            cudaStream_t s) {
+                            cudaStream_t s, int pix) {
     if (grid <= 0 || grid > gn_batch_capacity()) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -1098,7 +1116,12 @@ cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, gn_fused_batch, dev_items, dev_cta_item);
+    switch (pix) {
+        case 1: return cudaLaunchKernelEx(&cfg, gn_fused_batch<1>, dev_items, dev_cta_item);
+        case 2: return cudaLaunchKernelEx(&cfg, gn_fused_batch<2>, dev_items, dev_cta_item);
+        case 4: return cudaLaunchKernelEx(&cfg, gn_fused_batch<4>, dev_items, dev_cta_item);
+        default: return cudaLaunchKernelEx(&cfg, gn_fused_batch<0>, dev_items, dev_cta_item);
+    }
 }
 
 void launch_gn_schedule(yas_tracker *tr, cudaStream_t s) {

@@ -94,11 +94,14 @@ struct RaycastBuffers {
     int zw, zh;        // z-range map size: ceil(w/8), ceil(h/8)
     float *znear;      // zw*zh
     float *zfar;       // zw*zh
+    unsigned *queue;   // next pixel of the persistent march (reset with the z-range)
 };
 void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
                    const int *skip, cudaStream_t s);
-// `warps_x`: a 128-thread CTA's four 8x4-pixel warp tiles side by side in x
-// (1: 8x16 pixels, 2: 16x8, the default, 4: 32x4); the output is the same.
+// `warps_x` 1, 2 (the default), 4: one thread per pixel, a 128-thread CTA's
+// four 8x4-pixel warp tiles side by side in x (8x16, 16x8, 32x4 pixels);
+// 0: persistent warps taking 8x4-pixel tiles from a queue.  The output is
+// the same.
 void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
                   float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int warps_x = 2);
 void launch_vmap_to_depth(const float4 *vmap, int vpitch, float *depth, int dpitch, int w, int h,

@@ -15,7 +15,7 @@ namespace yas {
 // how a batched Gauss-Newton launch partitions the session's pixels, so it
 // fixes the session's summation order.
 struct LaunchShape {
-    int march_warps_x = 2;       // ray-march CTA: 4 warp tiles of 8x4 pixels, this many across
+    int march_warps_x = 2;       // ray march: 1, 2, 4 warp tiles across a CTA; 0 persistent (tile queue)
     int integrate_ctas = 0;      // integration grid (0: 152 x 8)
     int gn_pixels_per_cta = 32768;  // batched GN: one CTA per this many level-0 pixels
 };

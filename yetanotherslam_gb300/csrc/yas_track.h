@@ -153,7 +153,12 @@ void tracker_model(yas_tracker *tr, cudaStream_t s);  // model pyramid from ref 
 int gn_batch_ctas(const yas_tracker *tr, int pixels_per_cta = 32768);
 // descriptor of its current frame
 void gn_batch_item(yas_tracker *tr, int cta0, GNBatchItem *out, int pixels_per_cta = 32768);
+// the same with an explicit CTA count (1..kFusedMaxCtas)
+void gn_batch_item_ctas(yas_tracker *tr, int cta0, int nctas, GNBatchItem *out);
+// the batched kernel's pixels-per-thread variant for these (host) descriptors:
+// 1, 2, 4 (residuals in registers) or 0 (any share)
+int gn_batch_pix(const GNBatchItem *items, int n);
 int gn_batch_capacity();                                // co-resident CTAs of the batched launch
 cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *dev_cta_item, int grid,
-                            cudaStream_t s);
+                            cudaStream_t s, int pix);
 }  // namespace yas
