@@ -251,6 +251,7 @@ def run_gpu(args):
     cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
     served = run_served(100 + 1000 * rank) if args.served else None
     batched = run_batched(7 + 1000 * rank) if args.batched else None
+    large = run_large(args.large_frames) if args.large else None
 
     value = world * args.steps / (total_ms * 1e-3)
     line = {
@@ -282,6 +283,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "served": served,
         "batched": batched,
+        "large": large,
         "clocks": clk.summary(),
     }
     if rank == 0:
@@ -515,6 +517,114 @@ def run_batched(seed: int = 7):
             "batched_over_plain": round(t_fps / plain_fps, 2)}
 
 
+LARGE = {"frames": 2000, "width": 1280, "height": 720, "voxel_m": 0.004, "trunc_m": 0.012, "hash_slots": 1 << 23,
+         "max_blocks": 1 << 21, "tsdf": "fp16+u16", "seed": 5, "correction_frame": 1800,
+         "scene": "four rooms in a 12 x 4 x 12 m box (interior walls with doorways), 80 objects, "
+                  "a closed loop of radius 4.5 m over the 2000 frames",
+         "mesher_max_triangles": 40_000_000}
+
+
+def run_large(frames: int = 2000):
+    """C5: a 2000-frame 1280x720 loop through a four-room scene at 4 mm (2^23 slots, FP16 TSDF), inputs
+    resident in HBM: tracking + fusion of every frame; a seeded pose correction (a twist spread linearly
+    over frames 0..1800, as a loop closure would) and de-integration of all frames at their tracked poses
+    with re-integration at the corrected ones; full-map marching cubes."""
+    import ctypes as C
+
+    import torch
+
+    from yetanotherslam_gb300 import _lib as L
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import synth
+
+    cfg = LARGE
+    W, H = cfg["width"], cfg["height"]
+    K = synth.intrinsics(W, H)
+    sc = synth.Scene.rooms(seed=cfg["seed"], loop_frames=frames)
+    t0 = time.perf_counter()
+    dev, dm, gt = [], [], []
+    T0inv = None
+    for i in range(frames):
+        f = sc.render(i, W, H)
+        if T0inv is None:
+            T0inv = np.linalg.inv(f.Twc)
+        gt.append(T0inv @ f.Twc)
+        r = torch.from_numpy(f.rgb).cuda()
+        d = torch.from_numpy(f.depth.view(np.int16)).cuda()
+        dev.append((r, d))
+        # the session's conversion: (float)u16 * 0.001f
+        dm.append((d.to(torch.int32) & 0xFFFF).to(torch.float32) * 0.001)
+    torch.cuda.synchronize()
+    render_s = time.perf_counter() - t0
+    s = rf.Session(W, H, K, hash_slots=cfg["hash_slots"], max_blocks=cfg["max_blocks"], voxel_size=cfg["voxel_m"],
+                   trunc_dist=cfg["trunc_m"], voxel_format=rf.VOXEL_F16, num_levels=3, iterations=(10, 5, 3))
+    poses, bad = [], 0
+    t0 = time.perf_counter()
+    for i in range(frames):
+        st, T = s.process(*dev[i])
+        bad += int(st != 0)
+        poses.append(T)
+    track_s = time.perf_counter() - t0
+    m = s.map()
+    n_blocks = m.num_allocated()
+    # seeded correction, spread over frames 0..correction_frame
+    rng = np.random.default_rng(cfg["correction_frame"])
+    xi = np.concatenate([rng.normal(0, 0.02, 3), rng.normal(0, np.radians(0.5), 3)])
+    fixed = [se3_exp_np(xi * min(1.0, i / cfg["correction_frame"])) @ T for i, T in enumerate(poses)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(frames):
+        m.Defuse(dm[i], poses[i])
+        m.Fuse(dm[i], fixed[i])
+    torch.cuda.synchronize()
+    reint_s = time.perf_counter() - t0
+    errs = m.take_errors()
+    me = rf.MeshEngine(cfg["mesher_max_triangles"])
+    ntri = C.c_uint()
+    L.call("yas_mesher_meshify", me.handle, m.handle, C.byref(ntri))  # warm (allocations, tables)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    code = L.load().yas_mesher_meshify(me.handle, m.handle, C.byref(ntri))
+    torch.cuda.synchronize()
+    mc_s = time.perf_counter() - t0
+    nbytes = C.c_size_t()
+    L.call("yas_map_device_bytes", m.handle, C.byref(nbytes))
+    drift = pose_error_np(gt[-1], poses[-1])
+    loop = pose_error_np(poses[0], poses[-1])
+    s.close()
+    return {"config": cfg, "frames": frames, "render_s": round(render_s, 1),
+            "tracking_fusion_fps": round(frames / track_s, 1), "frame_status_nonzero": bad,
+            "blocks_allocated": n_blocks, "map_device_gb": round(nbytes.value / 1e9, 2),
+            "reintegration_frames_per_s": round(frames / reint_s, 1),
+            "reintegration_note": "per frame: de-integrate at the tracked pose, integrate at the corrected one",
+            "map_error_bits": errs,
+            "mesh_triangles": ntri.value, "mesh_status": code, "mesh_ms": round(mc_s * 1e3, 2),
+            "drift_vs_truth_last_frame": {"t_m": round(drift[0], 4), "r_rad": round(drift[1], 4)},
+            "loop_gap_first_last": {"t_m": round(loop[0], 4), "r_rad": round(loop[1], 4)}}
+
+
+def se3_exp_np(xi):
+    """exp of a twist (translation part, rotation part) as a 4x4 matrix (Rodrigues and the left Jacobian)."""
+    v, w = np.asarray(xi[:3], float), np.asarray(xi[3:], float)
+    th = float(np.linalg.norm(w))
+    Wx = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    if th < 1e-12:
+        R, V = np.eye(3) + Wx, np.eye(3) + 0.5 * Wx
+    else:
+        a, b = np.sin(th) / th, (1 - np.cos(th)) / th ** 2
+        R = np.eye(3) + a * Wx + b * Wx @ Wx
+        V = np.eye(3) + b * Wx + (th - np.sin(th)) / th ** 3 * Wx @ Wx
+    T = np.eye(4)
+    T[:3, :3], T[:3, 3] = R, V @ v
+    return T
+
+
+def pose_error_np(A, B):
+    E = np.linalg.inv(A) @ B
+    c = np.clip((np.trace(E[:3, :3]) - 1.0) / 2.0, -1.0, 1.0)
+    return float(np.linalg.norm(E[:3, 3])), float(np.arccos(c))
+
+
 def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
     import oracle
 
@@ -582,6 +692,8 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=8)
     ap.add_argument("--served", type=int, default=1, help="1: also measure 32 served sessions (C4)")
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
+    ap.add_argument("--large", type=int, default=0, help="1: also run the 2000-frame 1280x720 large map (C5)")
+    ap.add_argument("--large-frames", type=int, default=2000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

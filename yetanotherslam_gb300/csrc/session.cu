@@ -38,7 +38,11 @@ struct __align__(16) FrameState {
     int pad;
 };
 
-// Float pose pair of fs->Tcm, one lane per entry (lanes 0..11).
+// Float pose pair of fs->Tcm, one lane per entry (lanes 0..11).  The inverse
+// translation is rounded once per operation, in the order of the host's
+// pose_inverse (built without contraction), so a frame fused by the session
+// and the same frame given to yas_map_fuse_depth / yas_map_defuse_depth at the
+// returned pose use the same float pose.
 __device__ void publish_pose(FrameState *fs, int lane) {
     const double *T = fs->Tcm;
     if (lane < 12) {
@@ -48,7 +52,9 @@ __device__ void publish_pose(FrameState *fs, int lane) {
             fs->pp.Tinv.r[i * 3 + j] = (float)T[j * 4 + i];
         } else {
             fs->pp.T.t[i] = (float)T[i * 4 + 3];
-            fs->pp.Tinv.t[i] = (float)(-((T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7]) + T[2 * 4 + i] * T[11]));
+            const double s = __dadd_rn(__dadd_rn(__dmul_rn(T[0 * 4 + i], T[3]), __dmul_rn(T[1 * 4 + i], T[7])),
+                                       __dmul_rn(T[2 * 4 + i], T[11]));
+            fs->pp.Tinv.t[i] = (float)(-s);
         }
     }
 }

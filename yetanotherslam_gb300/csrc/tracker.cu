@@ -487,6 +487,7 @@ struct FusedArgs {
     int L, mode;
     float angle_th, dist_th;
     unsigned long long *rows;  // [2 parities][2 passes][kFusedMaxCtas][32] tagged words
+    float4 *res4;              // per-pixel residuals of the PIX == 0 schedule (level-0 sized)
     GNState *st;
 };
 
@@ -878,7 +879,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
 // The fused schedule of one tracker over the whole grid.
 template <int PIX>
 __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_constant__ FusedArgs a) {
-    gn_schedule<PIX>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, nullptr, a.st, blockIdx.x, gridDim.x);
+    gn_schedule<PIX>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, a.res4, a.st, blockIdx.x, gridDim.x);
 }
 
 // Fused schedules of a batch of trackers in one launch: CTA b runs for item
@@ -974,20 +975,22 @@ static cudaError_t launch_fused_pix(const FusedArgs &a, int grid, cudaStream_t s
 // Grid of the fused schedule: every co-resident 1024-thread CTA (one per SM),
 // at most kFusedMaxCtas (the rows the system fold covers).  Level l gives each CTA a
 // chunk of ceil(P_l / grid) pixels rounded up to a warp; `pix` is the smallest
-// compiled pixels-per-thread bound (1, 2 or 4) that covers level 0's chunk.
-// Returns false when none does (the per-iteration launches are used).
+// compiled pixels-per-thread bound (1, 2 or 4) that covers level 0's chunk,
+// or 0 (any chunk, residuals through global memory) when none does.  Returns
+// false without cooperative launch (the per-iteration launches are used).
 static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
     if (tr->fused_max_grid[0] < 0) {
         int dev = 0, sms = 0, coop = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        int nb[3] = {0, 0, 0};
+        int nb[4] = {0, 0, 0, 0};
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], gn_fused<1>, kFusedThreads, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], gn_fused<2>, kFusedThreads, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], gn_fused<4>, kFusedThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[3], gn_fused<0>, kFusedThreads, 0);
         cudaGetLastError();
-        for (int i = 0; i < 3; ++i) tr->fused_max_grid[i] = coop ? std::min(nb[i] * sms, kFusedMaxCtas) : 0;
+        for (int i = 0; i < 4; ++i) tr->fused_max_grid[i] = coop ? std::min(nb[i] * sms, kFusedMaxCtas) : 0;
     }
     const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
     const int pixes[3] = {1, 2, 4};
@@ -1000,6 +1003,12 @@ static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
             grid = g;
             return true;
         }
+    }
+    // larger frames (e.g. 1280x720 on 152 SMs): residuals through global memory
+    if (tr->fused_max_grid[3] > 0) {
+        pix = 0;
+        grid = tr->fused_max_grid[3];
+        return true;
     }
     return false;
 }
@@ -1037,10 +1046,13 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
     a.angle_th = tr->angle_th;
     a.dist_th = tr->dist_th;
     a.rows = tr->fused_rows;
+    a.res4 = tr->res4;
     a.st = tr->state;
     if (tr->hook) tr->hook(tr->hook_ctx, 30);
-    const cudaError_t e = pix == 1 ? launch_fused_pix<1>(a, grid, s)
-                                   : (pix == 2 ? launch_fused_pix<2>(a, grid, s) : launch_fused_pix<4>(a, grid, s));
+    const cudaError_t e = pix == 1   ? launch_fused_pix<1>(a, grid, s)
+                          : pix == 2 ? launch_fused_pix<2>(a, grid, s)
+                          : pix == 4 ? launch_fused_pix<4>(a, grid, s)
+                                     : launch_fused_pix<0>(a, grid, s);
     if (e != cudaSuccess) {
         // e.g. a device without cooperative launch: use the per-iteration launches
         cudaGetLastError();

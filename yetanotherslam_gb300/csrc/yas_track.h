@@ -115,7 +115,7 @@ struct yas_tracker {
     unsigned *counters = nullptr; // tickets: pass A grid + groups, then pass B grid + groups
     unsigned long long *fused_rows = nullptr;  // fused schedule: tagged per-CTA rows
     bool use_fused = true;        // one cooperative launch for the whole schedule
-    int fused_max_grid[3] = {-1, -1, -1};  // co-resident CTAs for 1, 2, 4 pixels per thread
+    int fused_max_grid[4] = {-1, -1, -1, -1};  // co-resident CTAs for 1, 2, 4 pixels per thread, and any
     yas::GNState *state = nullptr;
     yas::GNState *state_host = nullptr;  // pinned
     void *staging = nullptr;             // host-input staging (w*h*4 bytes)

@@ -33,6 +33,11 @@ def _load():
         lib.yas_synth_render.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
                                          C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.yas_synth_render.restype = None
+        lib.yas_synth_render_brute.argtypes = lib.yas_synth_render.argtypes
+        lib.yas_synth_render_brute.restype = None
+        lib.yas_synth_scene_init_rooms.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_double, C.c_double,
+                                                   C.c_double, C.c_double, C.c_int]
+        lib.yas_synth_scene_init_rooms.restype = C.c_int
         _synth = lib
     return _synth
 
@@ -60,6 +65,20 @@ class Scene:
             raise RuntimeError(f"scene placement failed ({rc})")
         self.seed = seed
 
+    @classmethod
+    def rooms(cls, seed: int = 1, n_objects: int = 80, size: tuple[float, float, float] = (12.0, 4.0, 12.0),
+              loop_radius: float = 4.5, loop_frames: int = 2000) -> "Scene":
+        """Four rooms (interior walls with doorways) and a closed loop through them that
+        returns to its start after `loop_frames` frames."""
+        lib = _load()
+        sc = cls.__new__(cls)
+        sc._buf = C.create_string_buffer(lib.yas_synth_scene_size())
+        rc = lib.yas_synth_scene_init_rooms(sc._buf, seed, n_objects, *size, loop_radius, loop_frames)
+        if rc != 0:
+            raise RuntimeError(f"scene placement failed ({rc})")
+        sc.seed = seed
+        return sc
+
     def pose(self, i: int) -> np.ndarray:
         out = np.zeros(12, dtype=np.float64)
         _load().yas_synth_pose(self._buf, i, out.ctypes.data)
@@ -67,15 +86,17 @@ class Scene:
         T[:3, :4] = out.reshape(3, 4)
         return T
 
-    def render(self, i: int, width: int = 640, height: int = 480, clean: bool = False):
+    def render(self, i: int, width: int = 640, height: int = 480, clean: bool = False, brute: bool = False):
+        """Frame i; `brute` tests every object for every pixel (no per-tile culling; same output)."""
         fx, fy, cx, cy = intrinsics(width, height)
         Twc = self.pose(i)
         m = np.ascontiguousarray(Twc[:3, :4].reshape(-1))
         rgb = np.empty((height, width, 3), dtype=np.uint8)
         depth = np.empty((height, width), dtype=np.uint16)
         cl = np.empty((height, width), dtype=np.float32) if clean else None
-        _load().yas_synth_render(self._buf, m.ctypes.data, width, height, fx, fy, cx, cy, i,
-                                 rgb.ctypes.data, depth.ctypes.data, cl.ctypes.data if clean else None)
+        fn = _load().yas_synth_render_brute if brute else _load().yas_synth_render
+        fn(self._buf, m.ctypes.data, width, height, fx, fy, cx, cy, i, rgb.ctypes.data, depth.ctypes.data,
+           cl.ctypes.data if clean else None)
         f = Frame(rgb, depth, Twc)
         if clean:
             return f, cl
