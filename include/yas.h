@@ -313,6 +313,35 @@ YAS_API int yas_gn_linearise_static(const yas_gn_level *level, const yas_pose *T
  * library's device buffers without linking the CUDA runtime itself. */
 YAS_API int yas_copy_to_host(void *dst, int dst_pitch, const void *src, int src_pitch, int width_bytes, int height);
 
+/* ---------------------------------------------------------------- ImageProc free functions
+ * RGBDFusion/include/ImageProc.h:8-24.  Device images (cv::cuda::GpuMat):
+ * pointer, size, row pitch in bytes; float, or float4 for vertex / normal
+ * maps.  Asynchronous on `stream`; outputs are written as the reference
+ * kernels write them (pixels the reference leaves untouched stay as they are). */
+/* PyrDownDepth (ImageProc.cu:166-187): dst(x, y) = src(2x, 2y) except dst's last row and column. */
+YAS_API int yas_pyr_down_depth(const float *src, int src_w, int src_h, int src_pitch, float *dst, int dst_w,
+                               int dst_h, int dst_pitch, void *stream);
+/* DepthToInvDepth (ImageProc.cu:141-164): 1/z for 0.2 < z < 8 m, else 0. */
+YAS_API int yas_depth_to_inv_depth(const float *depth, int w, int h, int pitch, float *inv_depth, int inv_pitch,
+                                   void *stream);
+/* ComputeVertexMap (ImageProc.cu:189-220): from inverse depth; w = -1 where invalid. */
+YAS_API int yas_compute_vertex_map(const float *inv_depth, int w, int h, int pitch, float *vmap, int vmap_pitch,
+                                   float invfx, float invfy, float cx, float cy, float cut_off, void *stream);
+/* ComputeNormalMap (ImageProc.cu:222-260): normalize((v(x,y+1) - v) x (v(x+1,y) - v)). */
+YAS_API int yas_compute_normal_map(const float *vmap, int w, int h, int pitch, float *nmap, int nmap_pitch,
+                                   void *stream);
+/* ComputeImageGradientCentralDifference (ImageProc.cu:7-40): 0.5 central differences, 0 on the border. */
+YAS_API int yas_image_gradient(const float *image, int w, int h, int pitch, float *gx, float *gy, int grad_pitch,
+                               void *stream);
+/* TransformReferencePoint (ImageProc.cu:42-78): points of an inverse-depth image
+ * moved by T: (R K^-1) (x, y, 1) z + t, R K^-1 formed in FP64 and rounded to FP32.
+ * K: row-major 3x3 double. */
+YAS_API int yas_transform_reference_point(const float *inv_depth, int w, int h, int pitch, float *vmap,
+                                          int vmap_pitch, const double *K, const yas_pose *T, void *stream);
+/* VMapToDepth (ImageProc.cu:262-286): z of valid vertices, else 0. */
+YAS_API int yas_vmap_to_depth(const float *vmap, int w, int h, int pitch, float *depth, int depth_pitch,
+                              void *stream);
+
 /* ---------------------------------------------------------------- shading
  * RenderScene(vmap, nmap, image), ImageProc.cu:128-139 (ImageProc.h:17): Phong
  * shading of a device vertex/normal map (float4, camera frame, the same row
@@ -321,6 +350,31 @@ YAS_API int yas_copy_to_host(void *dst, int dst_pitch, const void *src, int src_
  * (on_device = 1) or host memory (0, copied back before return). */
 YAS_API int yas_render_scene(const float *dev_vmap, const float *dev_nmap, int width, int height, int pitch_bytes,
                              const float *light, uint8_t *rgba, int out_pitch_bytes, int on_device, void *stream);
+
+/* ---------------------------------------------------------------- mesh canvas
+ * The viewer's mesh drawing (FullSystem/src/MapDrawer.cpp:159-234 with the GLSL
+ * program of :13-58), headless: submap meshes are shaded per vertex as the
+ * vertex shader does (light (5, 5, 5), viewer at the submap origin, in submap
+ * coordinates) and rasterised with a z-buffer into a device image: placed by
+ * Tmw (submap -> world, MapStruct::GetPose) and Tcw (world -> camera), pinhole
+ * intrinsics with pixel centres at integer coordinates, perspective-correct
+ * Gouraud interpolation, white background, triangles with a vertex nearer
+ * than 5 cm left out.  Meshes drawn after one another share the z-buffer. */
+typedef struct yas_canvas yas_canvas;
+YAS_API int yas_canvas_create(yas_canvas **out, int width, int height, const yas_intrinsics *K, void *stream);
+YAS_API int yas_canvas_destroy(yas_canvas *c);
+/* Empties the z-buffer (the image reads white). */
+YAS_API int yas_canvas_clear(yas_canvas *c);
+/* A triangle soup as MeshEngine writes it: 9 floats per triangle (submap
+ * metres) and the normal per vertex; host (on_device = 0) or device memory. */
+YAS_API int yas_canvas_draw_triangles(yas_canvas *c, const float *points, const float *normals, unsigned n_tris,
+                                      int on_device, const yas_pose *Tmw, const yas_pose *Tcw);
+/* The mesher's last mesh, from its device buffers (no copy to the host). */
+YAS_API int yas_canvas_draw_mesh(yas_canvas *c, yas_mesher *me, const yas_pose *Tmw, const yas_pose *Tcw);
+/* RGBA8 image and depth (metres, 0 where empty) of the z-buffer; either may be
+ * NULL; host (on_device = 0, copied back before return) or device memory. */
+YAS_API int yas_canvas_read(yas_canvas *c, uint8_t *rgba, int rgba_pitch, float *depth, int depth_pitch,
+                            int on_device);
 
 /* ---------------------------------------------------------------- session
  * One SLAM session: a submap, a raycaster and a tracker whose per-frame dense

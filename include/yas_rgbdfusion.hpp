@@ -8,7 +8,7 @@
  *   RayTraceEngine   RGBDFusion/include/RayTraceEngine.h:11-49
  *   MeshEngine       RGBDFusion/include/MeshEngine.h:8-24
  *   RGBDTracking     RGBDFusion/include/RGBDTracking.h:9-107
- *   RenderScene      RGBDFusion/include/ImageProc.h:17
+ *   ImageProc        RGBDFusion/include/ImageProc.h:8-24 (free functions)
  *
  * Types.  The reference passes Sophus::SE3d, Eigen::Matrix3f/3d, cv::Mat and
  * cv::cuda::GpuMat.  This header uses small stand-ins by default:
@@ -591,6 +591,67 @@ private:
 };
 
 /* ------------------------------------------------------------------ ImageProc */
+/* The free functions of ImageProc.h:8-24 on device images (GpuMat roles): the
+ * output image must be allocated by the caller with the input's size (or the
+ * pyramid level's, for PyrDownDepth); pixels the reference leaves unwritten
+ * keep their contents. */
+
+inline void require_device(const Image &a, int elem) {
+    if (!a.on_device || a.empty() || a.elem_bytes != elem) throw Error(YAS_ERR_BAD_ARG);
+}
+
+inline void PyrDownDepth(const Image &src, Image &dst) {
+    require_device(src, 4);
+    require_device(dst, 4);
+    check(yas_pyr_down_depth(static_cast<const float *>(src.data), src.cols, src.rows, (int)src.step,
+                             static_cast<float *>(dst.data), dst.cols, dst.rows, (int)dst.step, nullptr));
+}
+inline void ComputeVertexMap(const Image &depth_inv, Image &vmap, float invfx, float invfy, float cx, float cy,
+                             float cut_off) {
+    require_device(depth_inv, 4);
+    require_device(vmap, 16);
+    check(yas_compute_vertex_map(static_cast<const float *>(depth_inv.data), depth_inv.cols, depth_inv.rows,
+                                 (int)depth_inv.step, static_cast<float *>(vmap.data), (int)vmap.step, invfx, invfy, cx,
+                                 cy, cut_off, nullptr));
+}
+inline void ComputeNormalMap(const Image &vmap, Image &nmap) {
+    require_device(vmap, 16);
+    require_device(nmap, 16);
+    check(yas_compute_normal_map(static_cast<const float *>(vmap.data), vmap.cols, vmap.rows, (int)vmap.step,
+                                 static_cast<float *>(nmap.data), (int)nmap.step, nullptr));
+}
+inline void DepthToInvDepth(const Image &depth, Image &depth_inv) {
+    require_device(depth, 4);
+    require_device(depth_inv, 4);
+    check(yas_depth_to_inv_depth(static_cast<const float *>(depth.data), depth.cols, depth.rows, (int)depth.step,
+                                 static_cast<float *>(depth_inv.data), (int)depth_inv.step, nullptr));
+}
+inline void ComputeImageGradientCentralDifference(const Image &image, Image &gx, Image &gy) {
+    require_device(image, 4);
+    require_device(gx, 4);
+    require_device(gy, 4);
+    if (gx.step != gy.step) throw Error(YAS_ERR_BAD_ARG);
+    check(yas_image_gradient(static_cast<const float *>(image.data), image.cols, image.rows, (int)image.step,
+                             static_cast<float *>(gx.data), static_cast<float *>(gy.data), (int)gx.step, nullptr));
+}
+template <typename K3>
+inline void TransformReferencePoint(const Image &depth_inv, Image &vmap, const K3 &K, const SE3d &T) {
+    require_device(depth_inv, 4);
+    require_device(vmap, 16);
+    double Kd[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Kd[r * 3 + c] = (double)K(r, c);
+    const yas_pose p = to_pose(T);
+    check(yas_transform_reference_point(static_cast<const float *>(depth_inv.data), depth_inv.cols, depth_inv.rows,
+                                        (int)depth_inv.step, static_cast<float *>(vmap.data), (int)vmap.step, Kd, &p,
+                                        nullptr));
+}
+inline void VMapToDepth(const Image &vmap, Image &depth) {
+    require_device(vmap, 16);
+    require_device(depth, 4);
+    check(yas_vmap_to_depth(static_cast<const float *>(vmap.data), vmap.cols, vmap.rows, (int)vmap.step,
+                            static_cast<float *>(depth.data), (int)depth.step, nullptr));
+}
 
 /* RenderScene(vmap, nmap, image) (ImageProc.cu:128-139): RGBA8 into `image`
  * (host or device, rows x cols of the vertex map). */
@@ -609,6 +670,13 @@ inline void RenderScene(const Image &vmap, const Image &nmap, Image &image) {
 using yas::shim::MapStruct;
 using yas::shim::MeshEngine;
 using yas::shim::RayTraceEngine;
+using yas::shim::ComputeImageGradientCentralDifference;
+using yas::shim::ComputeNormalMap;
+using yas::shim::ComputeVertexMap;
+using yas::shim::DepthToInvDepth;
+using yas::shim::PyrDownDepth;
 using yas::shim::RenderScene;
 using yas::shim::RGBDTracking;
+using yas::shim::TransformReferencePoint;
+using yas::shim::VMapToDepth;
 #endif

@@ -49,6 +49,7 @@ _SIGS = {
     "orc_map_defuse": ([_P, _P, _I, _I, _P, _P], _I),
     "orc_map_fuse_map": ([_P, _P, _P, _P], _I),
     "orc_render_scene": ([_P, _P, _I, _I, _P, _P], None),
+    "orc_canvas_draw": ([_P, _P, C.c_uint, _P, _P, _P, _I, _I, _P], None),
     "orc_se3_exp": ([_P, _P], None),
     "orc_ldlt_solve6": ([_P, _P, _P], None),
     "orc_real_bytes": ([], _I),
@@ -265,6 +266,27 @@ class Session:
             return m.export()
         finally:
             m.h = None
+
+
+def canvas_draw(pts: np.ndarray, nrm: np.ndarray, Tmw, Tcw, K, w: int, h: int, keys: np.ndarray | None = None):
+    """MapDrawer's mesh program as a rasteriser: draws an (n, 9) triangle soup into
+    the 64-bit z-buffer `keys` (new, all empty, when None); returns keys."""
+    if keys is None:
+        keys = np.full((h, w), np.iinfo(np.uint64).max, dtype=np.uint64)
+    p = np.ascontiguousarray(pts, dtype=np.float32)
+    n = np.ascontiguousarray(nrm, dtype=np.float32)
+    k4 = np.ascontiguousarray(np.asarray(K, dtype=np.float32).reshape(-1)[:4])
+    lib().orc_canvas_draw(_ptr(p), _ptr(n), p.shape[0], _ptr(_pose(Tmw)), _ptr(_pose(Tcw)), _ptr(k4), w, h, _ptr(keys))
+    return keys
+
+
+def canvas_resolve(keys: np.ndarray):
+    """(rgba (h, w, 4) uint8 on a white background, depth (h, w) float32, 0 where empty)."""
+    empty = keys == np.iinfo(np.uint64).max
+    lo = np.where(empty, np.uint64(0xFFFFFFFF), keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    rgba = lo.view(np.uint8).reshape(keys.shape + (4,))
+    depth = np.where(empty, np.uint32(0), (keys >> np.uint64(32)).astype(np.uint32)).view(np.float32)
+    return rgba, depth
 
 
 def render_scene(vmap: np.ndarray, nmap: np.ndarray, light=(5.0, 5.0, 5.0)) -> np.ndarray:

@@ -67,6 +67,8 @@ void orc_raycast(orc_map *m, int w, int h, const float *K, const double *Tcm, fl
  * the number of triangles (writes at most cap). */
 /* RenderScene: Phong shading of a vertex/normal map (float4, w*h) into RGBA8. */
 void orc_render_scene(const float *vmap, const float *nmap, int w, int h, const float *light, unsigned char *rgba);
+void orc_canvas_draw(const float *pts, const float *nrm, unsigned ntris, const double *Tmw, const double *Tcw,
+                     const float *K4, int w, int h, uint64_t *keys);
 int orc_mesh(const orc_map *m, float *tris, float *normals, int *cases, int *cube_xyz, int cap);
 void orc_mc_tables(unsigned short *edge, signed char *tri, unsigned char *count);
 

@@ -853,3 +853,107 @@ void orc_render_scene(const float *vmap, const float *nmap, int w, int h, const 
         o[3] = 255;
     }
 }
+
+/* ---------------------------------------------------------------- mesh canvas
+ * MapDrawer's GLSL mesh program (FullSystem/src/MapDrawer.cpp:13-58, drawn by
+ * :159-234) restated as a z-buffered rasteriser: per-vertex shading in the
+ * submap frame, Tmw then Tcw, pinhole projection with pixel centres at
+ * integer coordinates, perspective-correct interpolation, depth test on
+ * (depth bits << 32 | RGBA).  Every operation is a single FP32 rounding in a
+ * fixed order (this file is built without contraction). */
+static float cv_dot(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static void cv_normalize(float v[3]) {
+    const float l = sqrtf(cv_dot(v, v));
+    if (!(l > 0.0f)) {
+        v[0] = v[1] = v[2] = 0.0f;
+        return;
+    }
+    v[0] = v[0] / l;
+    v[1] = v[1] / l;
+    v[2] = v[2] / l;
+}
+
+static float cv_shade(const float p[3], const float n[3]) {
+    float L[3] = {5.0f - p[0], 5.0f - p[1], 5.0f - p[2]};
+    float V[3] = {-p[0], -p[1], -p[2]};
+    cv_normalize(L);
+    cv_normalize(V);
+    const float nl = cv_dot(n, L);
+    const float k = 2.0f * nl;
+    float R[3] = {k * n[0] - L[0], k * n[1] - L[1], k * n[2] - L[2]};
+    cv_normalize(R);
+    const float rv = fmaxf(0.0f, cv_dot(R, V));
+    const float r2 = rv * rv, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8, r20 = r16 * r4;
+    const float i = (0.3f + 0.5f * fmaxf(0.0f, nl)) + 0.2f * r20;
+    return fminf(1.0f, fmaxf(0.0f, i));
+}
+
+static void cv_apply(const float A[12], const float x[3], float o[3]) {
+    for (int r = 0; r < 3; ++r) o[r] = ((A[r * 4] * x[0] + A[r * 4 + 1] * x[1]) + A[r * 4 + 2] * x[2]) + A[r * 4 + 3];
+}
+
+static float cv_edge(float ax, float ay, float bx, float by, float px, float py) {
+    return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+
+void orc_canvas_draw(const float *pts, const float *nrm, unsigned ntris, const double *Tmw, const double *Tcw,
+                     const float *K4, int w, int h, uint64_t *keys) {
+    float M[12], Vw[12];
+    for (int i = 0; i < 12; ++i) {
+        M[i] = (float)Tmw[i];
+        Vw[i] = (float)Tcw[i];
+    }
+    const float fx = K4[0], fy = K4[1], cx = K4[2], cy = K4[3];
+    for (unsigned t = 0; t < ntris; ++t) {
+        float u[3], v[3], iz[3], ioz[3];
+        int near = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float *p = pts + (size_t)t * 9 + k * 3, *q = nrm + (size_t)t * 9 + k * 3;
+            const float shade = cv_shade(p, q);
+            float pw[3], pc[3];
+            cv_apply(M, p, pw);
+            cv_apply(Vw, pw, pc);
+            near = near || !(pc[2] >= 0.05f);
+            u[k] = (fx * pc[0]) / pc[2] + cx;
+            v[k] = (fy * pc[1]) / pc[2] + cy;
+            iz[k] = 1.0f / pc[2];
+            ioz[k] = shade * iz[k];
+        }
+        if (near) continue;
+        const float area = cv_edge(u[0], v[0], u[1], v[1], u[2], v[2]);
+        if (!(area != 0.0f)) continue;
+        const float lim = 1.0e7f;
+        int x0 = (int)ceilf(fmaxf(-lim, fminf(fminf(u[0], u[1]), u[2])));
+        int x1 = (int)floorf(fminf(lim, fmaxf(fmaxf(u[0], u[1]), u[2])));
+        int y0 = (int)ceilf(fmaxf(-lim, fminf(fminf(v[0], v[1]), v[2])));
+        int y1 = (int)floorf(fminf(lim, fmaxf(fmaxf(v[0], v[1]), v[2])));
+        if (x0 < 0) x0 = 0;
+        if (y0 < 0) y0 = 0;
+        if (x1 > w - 1) x1 = w - 1;
+        if (y1 > h - 1) y1 = h - 1;
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const float px = (float)x, py = (float)y;
+                const float e0 = cv_edge(u[1], v[1], u[2], v[2], px, py);
+                const float e1 = cv_edge(u[2], v[2], u[0], v[0], px, py);
+                const float e2 = cv_edge(u[0], v[0], u[1], v[1], px, py);
+                const int in = area > 0.0f ? (e0 >= 0.0f && e1 >= 0.0f && e2 >= 0.0f)
+                                           : (e0 <= 0.0f && e1 <= 0.0f && e2 <= 0.0f);
+                if (!in) continue;
+                const float b0 = e0 / area, b1 = e1 / area, b2 = e2 / area;
+                const float wz = (b0 * iz[0] + b1 * iz[1]) + b2 * iz[2];
+                if (!(wz > 0.0f)) continue;
+                const float z = 1.0f / wz;
+                const float wi = (b0 * ioz[0] + b1 * ioz[1]) + b2 * ioz[2];
+                const float in01 = fminf(1.0f, fmaxf(0.0f, wi * z));
+                const uint32_t c = (uint32_t)floorf(in01 * 255.0f + 0.5f);
+                const uint32_t rgba = c | (c << 8) | (c << 16) | (255u << 24);
+                uint32_t zb;
+                memcpy(&zb, &z, 4);
+                const uint64_t key = ((uint64_t)zb << 32) | rgba;
+                uint64_t *dst = keys + (size_t)y * w + x;
+                if (key < *dst) *dst = key;
+            }
+    }
+}

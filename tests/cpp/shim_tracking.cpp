@@ -169,6 +169,26 @@ int main(int argc, char **argv) {
             for (int x = 0; x < rgba.cols * 4; ++x) rsum += rgba.ptr<uint8_t>(r)[x];
         std::fprintf(out, "render %d %d %llu\n", rgba.cols, rgba.rows, rsum);
 
+        // VMapToDepth (a free function) on the model vertex map, written into a
+        // device image the library owns and the run no longer needs (the
+        // tracker's level-0 inverse depth of the current frame)
+        {
+            const void *scratch = nullptr;
+            int sw = 0, sh = 0, sp = 0;
+            yas::shim::check(yas_tracker_level_buffer(tracker.handle(), 0, 3, &scratch, &sw, &sh, &sp));
+            Image dimg(scratch, sh, sw, 4, (size_t)sp, true);
+            VMapToDepth(Image(vm, lh, lw, 16, (size_t)vp, true), dimg);
+            std::vector<float> a((size_t)lw * lh), v4((size_t)lw * lh * 4);
+            yas::shim::check(yas_copy_to_host(a.data(), lw * 4, scratch, sp, lw * 4, lh));
+            yas::shim::check(yas_copy_to_host(v4.data(), lw * 16, vm, vp, lw * 16, lh));
+            int ok = 1;
+            for (size_t i = 0; i < a.size(); ++i) {
+                const float want = v4[4 * i + 3] > 0.0f ? v4[4 * i + 2] : 0.0f;
+                if (a[i] != want) ok = 0;
+            }
+            std::fprintf(out, "vmap_to_depth %d\n", ok);
+        }
+
         // GetReferenceDepth: the raw depth of the last Set*Depth call
         const Image raw = tracker.GetReferenceDepth();
         bool same = raw.rows == H && raw.cols == W;

@@ -59,3 +59,39 @@ def test_render_scene_matches_oracle(cuda):
     host = np.zeros((H, W, 4), np.uint8)
     L.call("yas_render_scene", ptrs[0], ptrs[1], W, H, W * 16, light, host.ctypes.data, W * 4, 0, None)
     assert np.array_equal(host, img)
+
+
+def test_mesh_canvas_matches_oracle(cuda):
+    """MapDrawer's mesh program (FullSystem/src/MapDrawer.cpp:13-58, 159-234) as a
+    rasteriser: two submap meshes drawn into one z-buffer, bit-exact against
+    the oracle's restatement (image and depth)."""
+    W, H = 320, 240
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, 4, W, H)
+    s = rf.Session(W, H, K, hash_slots=1 << 18, max_blocks=1 << 15)
+    T = None
+    for rgb, d16, _, _ in seq:
+        st, T = s.process(rgb, d16)
+        assert st == 0
+    me = rf.MeshEngine(2_000_000)
+    pts, nrm, _, _ = me.Meshify(s.map())
+    assert pts.shape[0] > 10000
+    Tcw = np.linalg.inv(T)
+    Tmw2 = np.eye(4)
+    c, sn = np.cos(0.3), np.sin(0.3)
+    Tmw2[:3, :3] = [[c, 0, sn], [0, 1, 0], [-sn, 0, c]]
+    Tmw2[:3, 3] = [0.4, 0.05, 0.3]
+    cv = rf.Canvas(W, H, K)
+    cv.draw_mesh(me, np.eye(4), Tcw)
+    cv.draw_triangles(pts, nrm, Tmw2, Tcw)
+    rgba, depth = cv.read()
+    keys = oracle.canvas_draw(pts, nrm, np.eye(4), Tcw, K, W, H)
+    keys = oracle.canvas_draw(pts, nrm, Tmw2, Tcw, K, W, H, keys)
+    ro, do = oracle.canvas_resolve(keys)
+    assert np.array_equal(rgba, ro) and np.array_equal(depth, do)
+    drawn = depth > 0
+    assert drawn.mean() > 0.3 and (rgba[~drawn] == 255).all()
+    assert len(np.unique(rgba[drawn][:, 0])) > 50
+    cv.clear()
+    rgba2, depth2 = cv.read()
+    assert (rgba2 == 255).all() and not depth2.any()

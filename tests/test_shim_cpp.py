@@ -171,6 +171,7 @@ def test_shim_tracking_matches_python_classes(cuda, tmp_path):
            W * 16, None, img.ctypes.data, W * 4, 0, None)
     assert got["render"] == [str(W), str(H), str(int(img.astype(np.uint64).sum()))]
     assert got["raw_depth"] == ["1"]
+    assert got["vmap_to_depth"] == ["1"]
     for name in ("curr_image.pfm", "last_image.pfm", "gx.pfm", "gy.pfm"):
         data = (tmp_path / name).read_bytes()
         head = f"Pf\n{W} {H}\n-1.0\n".encode()

@@ -119,6 +119,19 @@ _SIGS = {
     "yas_map_reset_visible": [_P],
     "yas_copy_to_host": [_P, _I, _P, _I, _I, _I],
     "yas_tracker_set_reduction": [_P, _I],
+    "yas_pyr_down_depth": [_P, _I, _I, _I, _P, _I, _I, _I, _P],
+    "yas_depth_to_inv_depth": [_P, _I, _I, _I, _P, _I, _P],
+    "yas_compute_vertex_map": [_P, _I, _I, _I, _P, _I, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _P],
+    "yas_compute_normal_map": [_P, _I, _I, _I, _P, _I, _P],
+    "yas_image_gradient": [_P, _I, _I, _I, _P, _P, _I, _P],
+    "yas_transform_reference_point": [_P, _I, _I, _I, _P, _I, _P, C.POINTER(Pose), _P],
+    "yas_vmap_to_depth": [_P, _I, _I, _I, _P, _I, _P],
+    "yas_canvas_create": [_PP, _I, _I, C.POINTER(Intrinsics), _P],
+    "yas_canvas_destroy": [_P],
+    "yas_canvas_clear": [_P],
+    "yas_canvas_draw_triangles": [_P, _P, _P, C.c_uint, _I, C.POINTER(Pose), C.POINTER(Pose)],
+    "yas_canvas_draw_mesh": [_P, _P, C.POINTER(Pose), C.POINTER(Pose)],
+    "yas_canvas_read": [_P, _P, _I, _P, _I, _I],
     "yas_map_defuse_depth": [_P, _P, _I, _I, _I, _I, C.POINTER(Pose)],
     "yas_raycaster_create": [_PP, _I, _I, C.POINTER(Intrinsics), _P],
     "yas_raycaster_destroy": [_P],

@@ -24,7 +24,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 
-CUDA_SOURCES = ["map.cu", "raycast.cu", "mesh.cu", "imgproc.cu", "tracker.cu", "capi.cu", "session.cu", "server.cu", "fusion.cu", "batch.cu"]
+CUDA_SOURCES = ["map.cu", "raycast.cu", "mesh.cu", "imgproc.cu", "tracker.cu", "capi.cu", "session.cu", "server.cu", "fusion.cu", "batch.cu", "canvas.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-lineinfo", "-O3", "-std=c++17",

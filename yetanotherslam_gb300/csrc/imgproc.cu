@@ -18,6 +18,8 @@
 //   model pyramid          RGBDTracking.cu:140-150 (SetReferenceModel); the reference runs
 //                          the float pyr-down on the float4 model (its coarse model levels
 //                          are unusable); here the intended float4 nearest pyr-down is used.
+#include <type_traits>
+
 #include "yas_internal.h"
 #include "yas_track.h"
 
@@ -275,3 +277,184 @@ void launch_render_scene(const float4 *vmap, const float4 *nmap, int vpitch, int
 }
 
 }  // namespace yas
+
+// ---------------------------------------------------------------- free functions of ImageProc.h
+// Standalone, pitched forms of the per-pixel functions the tracker fuses into
+// its pyramid kernels, for callers of the reference's free functions
+// (RGBDFusion/include/ImageProc.h:8-24).  One thread per pixel, 32x8 blocks.
+namespace yas {
+
+template <typename T>
+__device__ __forceinline__ T *row_at(T *base, int pitch_bytes, int y) {
+    return reinterpret_cast<T *>(reinterpret_cast<char *>(const_cast<typename std::remove_const<T>::type *>(base)) +
+                                 (size_t)y * pitch_bytes);
+}
+
+__global__ void free_pyrdown_depth_kernel(const float *src, int spitch, float *dst, int dw, int dh, int dpitch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    // PyrDownDepth_kernel: the last row and column are left as they are
+    if (x >= dw - 1 || y >= dh - 1) return;
+    row_at(dst, dpitch, y)[x] = row_at(src, spitch, 2 * y)[2 * x];
+}
+
+__global__ void free_inv_depth_kernel(const float *depth, int pitch, int w, int h, float *inv, int ipitch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    row_at(inv, ipitch, y)[x] = inv_depth_of(row_at(depth, pitch, y)[x]);
+}
+
+__global__ void free_vertex_map_kernel(const float *invd, int pitch, int w, int h, float4 *vmap, int vpitch,
+                                       float invfx, float invfy, float cx, float cy, float cut_off) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float invz = row_at(invd, pitch, y)[x];
+    const float z = 1.0f / invz;
+    float4 &o = row_at(vmap, vpitch, y)[x];
+    if (invz > 0.0f && z < cut_off)
+        o = make_float4(z * ((float)x - cx) * invfx, z * ((float)y - cy) * invfy, z, 1.0f);
+    else
+        o.w = -1.0f;  // ComputeVertexMap_kernel leaves x, y, z as they are
+}
+
+__global__ void free_normal_map_kernel(const float4 *vmap, int pitch, int w, int h, float4 *nmap, int npitch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float4 &o = row_at(nmap, npitch, y)[x];
+    if (x == w - 1 || y == h - 1) {
+        o.w = -1.0f;
+        return;
+    }
+    const float4 n = normal_of(row_at(vmap, pitch, y)[x], row_at(vmap, pitch, y)[x + 1], row_at(vmap, pitch, y + 1)[x]);
+    if (n.w > 0.0f)
+        o = n;
+    else
+        o.w = -1.0f;
+}
+
+__global__ void free_gradient_kernel(const float *src, int pitch, int w, int h, float *gx, float *gy, int gpitch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float *ox = row_at(gx, gpitch, y) + x, *oy = row_at(gy, gpitch, y) + x;
+    if (x < 1 || y < 1 || x > w - 2 || y > h - 2) {
+        *ox = *oy = 0.0f;
+    } else {
+        const float *r = row_at(src, pitch, y);
+        *ox = (r[x + 1] - r[x - 1]) * 0.5f;
+        *oy = (row_at(src, pitch, y + 1)[x] - row_at(src, pitch, y - 1)[x]) * 0.5f;
+    }
+}
+
+// TransformReferencePoint_kernel: RKinv (x, y, 1) z + t in FP32, Eigen's
+// row-by-row product order, one rounding per operation.
+__global__ void free_transform_points_kernel(const float *invd, int pitch, int w, int h, float4 *out, int opitch,
+                                             Rigid32 RK) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float zinv = row_at(invd, pitch, y)[x];
+    float4 &o = row_at(out, opitch, y)[x];
+    if (zinv > 0.0f) {
+        const float z = 1.0f / zinv, fx = (float)x, fy = (float)y;
+        float p[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            p[i] = __fadd_rn(__fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(RK.r[i * 3], fx), __fmul_rn(RK.r[i * 3 + 1], fy)),
+                                                 RK.r[i * 3 + 2]),
+                                       z),
+                             RK.t[i]);
+        o = make_float4(p[0], p[1], p[2], 1.0f);
+    } else {
+        o = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    }
+}
+
+}  // namespace yas
+
+using namespace yas;
+
+namespace {
+inline dim3 grid_of(int w, int h) { return dim3((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8)); }
+inline bool bad_img(const void *p, int w, int h, int pitch, int elem) {
+    return !p || w <= 0 || h <= 0 || pitch < w * elem || (pitch % elem) != 0;
+}
+}  // namespace
+
+extern "C" {
+
+YAS_API int yas_pyr_down_depth(const float *src, int src_w, int src_h, int src_pitch, float *dst, int dst_w,
+                               int dst_h, int dst_pitch, void *stream) {
+    if (bad_img(src, src_w, src_h, src_pitch, 4) || bad_img(dst, dst_w, dst_h, dst_pitch, 4) ||
+        2 * (dst_w - 2) >= src_w || 2 * (dst_h - 2) >= src_h)
+        return YAS_ERR_BAD_ARG;
+    free_pyrdown_depth_kernel<<<grid_of(dst_w, dst_h), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+        src, src_pitch, dst, dst_w, dst_h, dst_pitch);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_depth_to_inv_depth(const float *depth, int w, int h, int pitch, float *inv_depth, int inv_pitch,
+                                   void *stream) {
+    if (bad_img(depth, w, h, pitch, 4) || bad_img(inv_depth, w, h, inv_pitch, 4)) return YAS_ERR_BAD_ARG;
+    free_inv_depth_kernel<<<grid_of(w, h), dim3(32, 8), 0, (cudaStream_t)stream>>>(depth, pitch, w, h, inv_depth,
+                                                                                   inv_pitch);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_compute_vertex_map(const float *inv_depth, int w, int h, int pitch, float *vmap, int vmap_pitch,
+                                   float invfx, float invfy, float cx, float cy, float cut_off, void *stream) {
+    if (bad_img(inv_depth, w, h, pitch, 4) || bad_img(vmap, w, h, vmap_pitch, 16)) return YAS_ERR_BAD_ARG;
+    free_vertex_map_kernel<<<grid_of(w, h), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+        inv_depth, pitch, w, h, reinterpret_cast<float4 *>(vmap), vmap_pitch, invfx, invfy, cx, cy, cut_off);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_compute_normal_map(const float *vmap, int w, int h, int pitch, float *nmap, int nmap_pitch,
+                                   void *stream) {
+    if (bad_img(vmap, w, h, pitch, 16) || bad_img(nmap, w, h, nmap_pitch, 16)) return YAS_ERR_BAD_ARG;
+    free_normal_map_kernel<<<grid_of(w, h), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(vmap), pitch, w, h, reinterpret_cast<float4 *>(nmap), nmap_pitch);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_image_gradient(const float *image, int w, int h, int pitch, float *gx, float *gy, int grad_pitch,
+                               void *stream) {
+    if (bad_img(image, w, h, pitch, 4) || bad_img(gx, w, h, grad_pitch, 4) || bad_img(gy, w, h, grad_pitch, 4))
+        return YAS_ERR_BAD_ARG;
+    free_gradient_kernel<<<grid_of(w, h), dim3(32, 8), 0, (cudaStream_t)stream>>>(image, pitch, w, h, gx, gy,
+                                                                                  grad_pitch);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_transform_reference_point(const float *inv_depth, int w, int h, int pitch, float *vmap,
+                                          int vmap_pitch, const double *K, const yas_pose *T, void *stream) {
+    if (bad_img(inv_depth, w, h, pitch, 4) || bad_img(vmap, w, h, vmap_pitch, 16) || !K || !T) return YAS_ERR_BAD_ARG;
+    // R * K^-1 in FP64, then rounded to FP32 (TransformReferencePoint, ImageProc.cu:64-78)
+    const double fx = K[0], fy = K[4], cx = K[2], cy = K[5];
+    if (!(fx != 0.0 && fy != 0.0)) return YAS_ERR_BAD_ARG;
+    const double Ki[9] = {1.0 / fx, 0.0, -cx / fx, 0.0, 1.0 / fy, -cy / fy, 0.0, 0.0, 1.0};
+    Rigid32 RK;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            RK.r[i * 3 + j] = (float)((T->m[i * 4 + 0] * Ki[0 * 3 + j] + T->m[i * 4 + 1] * Ki[1 * 3 + j]) +
+                                      T->m[i * 4 + 2] * Ki[2 * 3 + j]);
+        RK.t[i] = (float)T->m[i * 4 + 3];
+    }
+    free_transform_points_kernel<<<grid_of(w, h), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+        inv_depth, pitch, w, h, reinterpret_cast<float4 *>(vmap), vmap_pitch, RK);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+YAS_API int yas_vmap_to_depth(const float *vmap, int w, int h, int pitch, float *depth, int depth_pitch,
+                              void *stream) {
+    if (bad_img(vmap, w, h, pitch, 16) || bad_img(depth, w, h, depth_pitch, 4)) return YAS_ERR_BAD_ARG;
+    launch_vmap_to_depth(reinterpret_cast<const float4 *>(vmap), pitch / 16, depth, depth_pitch / 4, w, h,
+                         (cudaStream_t)stream);
+    YAS_TRY_CUDA(cudaGetLastError());
+    return YAS_OK;
+}
+
+}  // extern "C"

@@ -302,16 +302,15 @@ __device__ __forceinline__ float4 ray_finish(VoxelReader<FMT> &rd, float rstep, 
 }
 
 // One thread per pixel; each warp a compact 8x4 tile, so its rays travel
-// similar depths; the CTA's four warp tiles lie WX across and 4/WX down
-// (a CTA covers 8WX x 16/WX pixels).
-template <int FMT, int WX>
-__global__ void __launch_bounds__(128) march_kernel(MapDev m, Cam cam, const PosePair *P,
-                                                    const float *__restrict__ znear,
-                                                    const float *__restrict__ zfar, int zw, float4 *vmap,
-                                                    int vpitch, const int *skip) {
+// similar depths; the CTA's WX x WY warp tiles cover 8WX x 4WY pixels.
+template <int FMT, int WX, int WY>
+__global__ void __launch_bounds__(32 * WX * WY) march_kernel(MapDev m, Cam cam, const PosePair *P,
+                                                             const float *__restrict__ znear,
+                                                             const float *__restrict__ zfar, int zw, float4 *vmap,
+                                                             int vpitch, const int *skip) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * (8 * WX) + (warp % WX) * 8 + (lane & 7);
-    const int y = blockIdx.y * (16 / WX) + (warp / WX) * 4 + (lane >> 3);
+    const int y = blockIdx.y * (4 * WY) + (warp / WX) * 4 + (lane >> 3);
     if (x >= cam.w || y >= cam.h) return;
     float4 out = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
                              -1.0f);
@@ -436,36 +435,35 @@ static void launch_march_persistent(const MapDev &m, int fmt, const Cam &cam, co
     }
 }
 
-template <int WX>
-static void launch_march_wx(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
-                            float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
-    dim3 grid((cam.w + 8 * WX - 1) / (8 * WX), (cam.h + 16 / WX - 1) / (16 / WX));
+template <int WX, int WY>
+static void launch_march_tile(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
+                              float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s) {
+    dim3 grid((cam.w + 8 * WX - 1) / (8 * WX), (cam.h + 4 * WY - 1) / (4 * WY));
+    const int threads = 32 * WX * WY;
     switch (fmt) {
         case YAS_VOXEL_F32:
-            march_kernel<YAS_VOXEL_F32, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                 vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_F32, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                         vmap_pitch_elems, skip);
             break;
         case YAS_VOXEL_F16:
-            march_kernel<YAS_VOXEL_F16, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                 vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_F16, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                         vmap_pitch_elems, skip);
             break;
         default:
-            march_kernel<YAS_VOXEL_S24, WX><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                 vmap_pitch_elems, skip);
+            march_kernel<YAS_VOXEL_S24, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                         vmap_pitch_elems, skip);
             break;
     }
 }
 
 void launch_march(const MapDev &m, int fmt, const Cam &cam, const PosePair *P, const RaycastBuffers &rb,
-                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int warps_x) {
-    if (warps_x == 0)
-        launch_march_persistent(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
-    else if (warps_x == 1)
-        launch_march_wx<1>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
-    else if (warps_x == 4)
-        launch_march_wx<4>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
-    else
-        launch_march_wx<2>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s);
+                  float4 *vmap, int vmap_pitch_elems, const int *skip, cudaStream_t s, int tile) {
+    switch (tile) {
+        case 0: launch_march_persistent(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s); break;
+        case 1: launch_march_tile<1, 4>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s); break;
+        case 4: launch_march_tile<4, 1>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s); break;
+        default: launch_march_tile<2, 2>(m, fmt, cam, P, rb, vmap, vmap_pitch_elems, skip, s); break;
+    }
 }
 
 __global__ void vmap_to_depth_kernel(const float4 *vmap, int vpitch, float *depth, int dpitch, int w,

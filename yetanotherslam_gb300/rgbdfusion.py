@@ -489,3 +489,40 @@ class Session:
         h = C.c_void_p()
         L.call("yas_session_tracker", self.handle, C.byref(h))
         L.call("yas_tracker_set_reduction", h, int(compensated))
+
+
+class Canvas:
+    """Headless drawing of submap meshes (MapDrawer's mesh program) into an RGBA image."""
+
+    def __init__(self, width: int, height: int, K, stream: int | None = None):
+        self.w, self.h = width, height
+        self.handle = C.c_void_p()
+        L.call("yas_canvas_create", C.byref(self.handle), width, height, C.byref(_intr(K)), stream)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.call("yas_canvas_destroy", self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+    def clear(self) -> None:
+        L.call("yas_canvas_clear", self.handle)
+
+    def draw_mesh(self, mesher: MeshEngine, Tmw, Tcw) -> None:
+        """The mesher's last mesh, placed by Tmw (submap -> world) and seen from Tcw (world -> camera)."""
+        L.call("yas_canvas_draw_mesh", self.handle, mesher.handle, C.byref(L.pose_from(Tmw)), C.byref(L.pose_from(Tcw)))
+
+    def draw_triangles(self, points, normals, Tmw, Tcw) -> None:
+        p = np.ascontiguousarray(points, dtype=np.float32)
+        n = np.ascontiguousarray(normals, dtype=np.float32)
+        L.call("yas_canvas_draw_triangles", self.handle, p.ctypes.data, n.ctypes.data, p.shape[0], 0,
+               C.byref(L.pose_from(Tmw)), C.byref(L.pose_from(Tcw)))
+
+    def read(self):
+        """(rgba (h, w, 4) uint8, depth (h, w) float32 metres, 0 where empty)."""
+        rgba = np.zeros((self.h, self.w, 4), np.uint8)
+        depth = np.zeros((self.h, self.w), np.float32)
+        L.call("yas_canvas_read", self.handle, rgba.ctypes.data, self.w * 4, depth.ctypes.data, self.w * 4, 0)
+        return rgba, depth
