@@ -418,7 +418,7 @@ BATCHED = {"submaps": 16, "resolutions": [[320, 240], [480, 360], [640, 480]], "
            "calibration_frames": 4}
 
 
-def run_batched(seed: int = 7):
+def run_batched(seed: int = 7, only_pass: bool = False):
     """C3: 16 keyframe submaps of uneven size (a seeded mix of 320x240 / 480x360 / 640x480, 5 or 8 mm
     voxels, 5-60 frames each), inputs resident in HBM, stepped by yas_batch (one graph launch per step,
     one batched GN launch) with autotuned launch shapes; against the same submaps run one after the
@@ -467,6 +467,11 @@ def run_batched(seed: int = 7):
             s.close()
         return frames, total_ms, wall, bad, kernels
 
+    if only_pass:  # one batched pass with the default tuning (for profiling)
+        run_batch(None)
+        f, ms, wall, bad, kernels = run_batch(None)
+        return {"submap_frames": f, "batched_fps_device": round(f / (ms * 1e-3), 1), "kernels_per_step": kernels,
+                "frame_status_nonzero": bad}
     # autotune on scratch copies, from each submap's first frames
     ss = sessions()
     b = batching.Batch(ss)
@@ -540,7 +545,8 @@ def run_large(frames: int = 2000):
     cfg = LARGE
     W, H = cfg["width"], cfg["height"]
     K = synth.intrinsics(W, H)
-    sc = synth.Scene.rooms(seed=cfg["seed"], loop_frames=frames)
+    # the loop is always the full 2000-frame one; a shorter run is a prefix of it
+    sc = synth.Scene.rooms(seed=cfg["seed"], loop_frames=cfg["frames"])
     t0 = time.perf_counter()
     dev, dm, gt = [], [], []
     T0inv = None
@@ -581,7 +587,7 @@ def run_large(frames: int = 2000):
     errs = m.take_errors()
     me = rf.MeshEngine(cfg["mesher_max_triangles"])
     ntri = C.c_uint()
-    L.call("yas_mesher_meshify", me.handle, m.handle, C.byref(ntri))  # warm (allocations, tables)
+    L.load().yas_mesher_meshify(me.handle, m.handle, C.byref(ntri))  # warm (allocations, tables)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     code = L.load().yas_mesher_meshify(me.handle, m.handle, C.byref(ntri))
@@ -694,9 +700,17 @@ def main():
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
     ap.add_argument("--large", type=int, default=0, help="1: also run the 2000-frame 1280x720 large map (C5)")
     ap.add_argument("--large-frames", type=int, default=2000)
+    ap.add_argument("--leg", choices=["served", "batched", "batched-pass", "large"], default=None,
+                    help="run only this workload and print its result (for profiling one leg)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.leg:
+        fn = {"served": lambda: run_served(100), "batched": lambda: run_batched(7),
+              "batched-pass": lambda: run_batched(7, only_pass=True),
+              "large": lambda: run_large(args.large_frames)}[args.leg]
+        print(json.dumps({"leg": args.leg, "result": fn()}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
