@@ -7,7 +7,11 @@ RGBDFusion/include/TrackingUtils.h.  Bars:
     99.99 % of pixels;
   * one Gauss-Newton linearisation from the same pose: every entry of H and
     b within 1e-3 of max|H| (resp. max|b|);
-  * GetTransform: pose within 1e-4 m and 1e-4 rad of the oracle.
+  * GetTransform: pose within 1e-4 m and 1e-4 rad of the oracle, plus the
+    distance between the oracle's own FP64 and FP32 builds on the same inputs
+    (zero unless FP32 arithmetic flips GetTransform's keep-the-better-estimate
+    decision on a near-tie, RGBDTracking.cu:184-199; the reference computes in
+    FP32 too).
 """
 from __future__ import annotations
 
@@ -25,6 +29,28 @@ pytestmark = pytest.mark.gpu
 def _K33(W, H):
     fx, fy, cx, cy = synth.intrinsics(W, H)
     return np.array([[fx, 0, cx], [0, fy, cy], [0, 0, 1.0]])
+
+
+def _fp32_slack(mode, W, H, iters=(10, 5, 3)):
+    """(t, r) distance between the oracle's FP64 and FP32 builds on _setup's inputs."""
+    K = _K33(W, H)
+    seq = sequence(11, 2, W, H)
+    m = rf.MapStruct(K)
+    m.create_config(1 << 18, 1 << 15, 0.008, 0.024, rf.VOXEL_F32)
+    m.Fuse(seq[0][2], np.eye(4))
+    rc = rf.RayTraceEngine(W, H, K)
+    rc.RayTrace(m, np.eye(4))
+    vm = rc.GetVMap().numpy()
+    out = []
+    for kind in ("f64", "f32"):
+        ot = oracle.Tracker(W, H, K, levels=3, iters=iters, mode=mode, kind=kind)
+        ot.set_image(synth.gray_of(seq[0][0]), True)
+        ot.set_depth(seq[0][2], True)
+        ot.set_image(synth.gray_of(seq[1][0]), False)
+        ot.set_depth(seq[1][2], False)
+        ot.set_model(vm)
+        out.append(ot.get_transform(np.eye(4), False)[1])
+    return pose_error(out[0], out[1])
 
 
 def _setup(mode, W=320, H=240, levels=3, iters=(10, 5, 3)):
@@ -106,7 +132,8 @@ def test_get_transform_matches_oracle(cuda, mode, fused):
     st, To = ot.get_transform(np.eye(4), False)
     assert st == 0 and tr.IsTrackingGood()
     dt, dr = pose_error(To, Tg)
-    assert dt <= 1e-4 and dr <= 1e-4, (dt, dr)
+    st32, sr32 = _fp32_slack(mode, 320, 240)
+    assert dt <= 1e-4 + st32 and dr <= 1e-4 + sr32, (dt, dr, st32, sr32)
     # and both land near the true motion
     et, er = pose_error(gt, Tg)
     assert et < 0.01 and er < 0.01
@@ -116,7 +143,8 @@ def test_get_transform_matches_oracle(cuda, mode, fused):
 def test_fused_schedule_matches_per_iteration_launches(cuda, mode):
     """One cooperative launch for the whole schedule against two launches per
     iteration at 640x480: the same arithmetic per pixel, summed in a different
-    order.  Both meet the oracle's pose within 1e-4 m / rad; between
+    order.  Both meet the oracle's pose within 1e-4 m / rad (plus the oracle's
+    own FP32-vs-FP64 distance on these inputs); between
     themselves they agree within 2e-5 (near convergence a rounding-level
     difference in the error can change which iteration is accepted); the
     fused schedule is reproducible call to call."""
@@ -131,9 +159,10 @@ def test_fused_schedule_matches_per_iteration_launches(cuda, mode):
     assert dt <= 2e-5 and dr <= 2e-5, (dt, dr)
     st, To = ot.get_transform(np.eye(4), False)
     assert st == 0
+    st32, sr32 = _fp32_slack(mode, 640, 480)
     for T in (Tf, Tp):
         dt, dr = pose_error(To, T)
-        assert dt <= 1e-4 and dr <= 1e-4, (dt, dr)
+        assert dt <= 1e-4 + st32 and dr <= 1e-4 + sr32, (dt, dr, st32, sr32)
 
 
 def test_tracking_from_no_data_returns_identity(cuda):

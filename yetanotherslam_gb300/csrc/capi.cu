@@ -890,8 +890,11 @@ YAS_API int yas_raycaster_create(yas_raycaster **out, int width, int height, con
     rc->rb.zw = (width + 7) / 8;
     rc->rb.zh = (height + 7) / 8;
     const size_t nz = (size_t)rc->rb.zw * rc->rb.zh;
+    rc->rb.fw = (width + 3) / 4;
+    rc->rb.fh = (height + 3) / 4;
     if (cudaMalloc(&rc->rb.znear, nz * 4) != cudaSuccess || cudaMalloc(&rc->rb.zfar, nz * 4) != cudaSuccess ||
         cudaMalloc(&rc->rb.queue, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&rc->rb.fnear, (size_t)rc->rb.fw * rc->rb.fh * 4) != cudaSuccess ||
         cudaMalloc(&rc->vmap, (size_t)width * height * 16) != cudaSuccess ||
         cudaMalloc(&rc->depth_tmp, (size_t)width * height * 4) != cudaSuccess ||
         cudaMalloc(&rc->pose_dev, sizeof(PosePair)) != cudaSuccess) {
@@ -910,6 +913,7 @@ YAS_API int yas_raycaster_destroy(yas_raycaster *rc) {
     cudaFree(rc->rb.znear);
     cudaFree(rc->rb.zfar);
     cudaFree(rc->rb.queue);
+    cudaFree(rc->rb.fnear);
     cudaFree(rc->vmap);
     cudaFree(rc->depth_tmp);
     cudaFree(rc->pose_dev);

@@ -27,11 +27,13 @@
 
 namespace yas {
 
-__global__ void zrange_reset_kernel(float *znear, float *zfar, int n, unsigned *n_render, unsigned *queue) {
+__global__ void zrange_reset_kernel(float *znear, float *zfar, int n, unsigned *n_render, unsigned *queue,
+                                    float *fnear, int nf) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         znear[i] = 100.0f;
         zfar[i] = 0.0f;
     }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) fnear[i] = 100.0f;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *n_render = 0;
         *queue = 0u;
@@ -51,7 +53,7 @@ __device__ __forceinline__ int clamp_ceil(float v) {
 
 __global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, const PosePair *P,
                                                           float *znear, float *zfar, int zw, int zh,
-                                                          const int *skip) {
+                                                          const int *skip, float *fnear, int fw, int fh) {
     if (skip && *skip) return;
     const unsigned nvis = *(volatile unsigned *)&m.hdr->n_visible;
     const Rigid32 Tinv = P->Tinv;
@@ -61,18 +63,42 @@ __global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, con
         unpack_key(m.block_keys[m.visible[j]], bx, by, bz);
         int ulx = zw, uly = zh, lrx = -1, lry = -1;
         float zmin = m.depth_max, zmax = m.depth_min;
+        float pu0 = 1e30f, pu1 = -1e30f, pv0 = 1e30f, pv1 = -1e30f;
+        bool behind = false;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             float3 p = rigid_exact(Tinv, (float)(bx + (c & 1)) * scale, (float)(by + ((c >> 1) & 1)) * scale,
                                    (float)(bz + ((c >> 2) & 1)) * scale);
-            float u = (cam.fx * p.x / p.z + cam.cx) / 8.0f;
-            float v = (cam.fy * p.y / p.z + cam.cy) / 8.0f;
+            const float pu = cam.fx * p.x / p.z + cam.cx, pv = cam.fy * p.y / p.z + cam.cy;
+            float u = pu / 8.0f;
+            float v = pv / 8.0f;
             ulx = min(ulx, clamp_floor(u));
             uly = min(uly, clamp_floor(v));
             lrx = max(lrx, clamp_ceil(u));
             lry = max(lry, clamp_ceil(v));
             zmin = fminf(zmin, p.z);
             zmax = fmaxf(zmax, p.z);
+            behind = behind || !(p.z > 1e-3f);
+            pu0 = fminf(pu0, pu);
+            pu1 = fmaxf(pu1, pu);
+            pv0 = fminf(pv0, pv);
+            pv1 = fmaxf(pv1, pv);
+        }
+        // Fine near bound (not a reference quantity; the march uses it only to
+        // jump over samples that lie before every visible block along the ray):
+        // the block's projected box widened by a pixel, or the whole image when a
+        // corner is not in front of the camera.
+        if (zmax >= m.depth_min) {
+            int fx0 = 0, fy0 = 0, fx1 = fw - 1, fy1 = fh - 1;
+            if (!behind) {
+                fx0 = max(fx0, clamp_floor((pu0 - 1.0f) * 0.25f));
+                fy0 = max(fy0, clamp_floor((pv0 - 1.0f) * 0.25f));
+                fx1 = min(fx1, clamp_floor((pu1 + 1.0f) * 0.25f));
+                fy1 = min(fy1, clamp_floor((pv1 + 1.0f) * 0.25f));
+            }
+            const int fz = __float_as_int(fmaxf(fminf(zmin, m.depth_max), 0.0f));
+            for (int y = fy0; y <= fy1; ++y)
+                for (int x = fx0; x <= fx1; ++x) atomicMin(reinterpret_cast<int *>(fnear) + y * fw + x, fz);
         }
         ulx = max(ulx, 0);
         uly = max(uly, 0);
@@ -94,9 +120,11 @@ __global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, con
 
 void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
                    const int *skip, cudaStream_t s) {
-    int n = rb.zw * rb.zh;
-    zrange_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render, rb.queue);
-    zrange_fill_kernel<<<152 * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip);
+    const int n = rb.zw * rb.zh, nf = rb.fw * rb.fh;
+    zrange_reset_kernel<<<(std::max(n, nf) + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render,
+                                                                      rb.queue, rb.fnear, nf);
+    zrange_fill_kernel<<<152 * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip, rb.fnear, rb.fw,
+                                               rb.fh);
 }
 
 // Block-pointer cache of one ray.
@@ -207,9 +235,13 @@ struct RayState {
 };
 
 // Ray of pixel (x, y) between the tile's z-range bounds zn..zf; false when the
-// tile has no range (the pixel is a miss).
-__device__ __forceinline__ bool ray_setup(const Cam &cam, const Rigid32 &T, float vsinv, float zn, float zf, int x,
-                                          int y, RayState &R) {
+// tile has no range (the pixel is a miss).  zfine: the nearest visible block
+// whose projected box covers the pixel's 4x4 neighbourhood.  The march starts
+// at zn as the reference's does; every sample before zfine lies outside every
+// visible block, reads "unobserved" and advances one voxel, so those samples
+// are taken in one move (two are kept as margin against rounding).
+__device__ __forceinline__ bool ray_setup(const Cam &cam, const Rigid32 &T, float vsinv, float zn, float zf,
+                                          float zfine, int x, int y, RayState &R) {
     if (zn < FLT_EPSILON || zf < FLT_EPSILON || isnan(zn) || isnan(zf)) return false;
     const float ux = cam.invfx * ((float)x - cam.cx), uy = cam.invfy * ((float)y - cam.cy);
     const float3 pn = make_float3(ux * zn, uy * zn, zn);
@@ -230,6 +262,14 @@ __device__ __forceinline__ bool ray_setup(const Cam &cam, const Rigid32 &T, floa
     R.skipped = kEmptyKey;
     R.sdf = 1.0f;
     R.valid = false;
+    if (zfine > zn) {
+        const float k = sqrtf(ux * ux + uy * uy + 1.0f) * vsinv;  // voxels of ray per metre of depth
+        const float n = floorf(fminf(zfine * k, R.dist_e) - R.dist_s) - 2.0f;
+        if (n >= 1.0f) {
+            R.r = make_float3(R.r.x + n * dir.x, R.r.y + n * dir.y, R.r.z + n * dir.z);
+            R.dist_s += n;
+        }
+    }
     return true;
 }
 
@@ -307,7 +347,8 @@ template <int FMT, int WX, int WY>
 __global__ void __launch_bounds__(32 * WX * WY) march_kernel(MapDev m, Cam cam, const PosePair *P,
                                                              const float *__restrict__ znear,
                                                              const float *__restrict__ zfar, int zw, float4 *vmap,
-                                                             int vpitch, const int *skip) {
+                                                             int vpitch, const int *skip,
+                                                             const float *__restrict__ fnear, int fw) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * (8 * WX) + (warp % WX) * 8 + (lane & 7);
     const int y = blockIdx.y * (4 * WY) + (warp / WX) * 4 + (lane >> 3);
@@ -319,7 +360,7 @@ __global__ void __launch_bounds__(32 * WX * WY) march_kernel(MapDev m, Cam cam, 
         const float rstep = m.trunc / m.voxel_size;
         RayState R;
         if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)), __ldg(zfar + (y >> 3) * zw + (x >> 3)),
-                      x, y, R)) {
+                      __ldg(fnear + (y >> 2) * fw + (x >> 2)), x, y, R)) {
             VoxelReader<FMT> rd(m);
             while (!ray_step(rd, rstep, R)) {
             }
@@ -339,7 +380,8 @@ __global__ void __launch_bounds__(128) march_persistent_kernel(MapDev m, Cam cam
                                                                const float *__restrict__ znear,
                                                                const float *__restrict__ zfar, int zw, float4 *vmap,
                                                                int vpitch, const int *skip, unsigned *queue,
-                                                               unsigned total) {
+                                                               unsigned total, const float *__restrict__ fnear,
+                                                               int fw) {
     const unsigned lane = lane_id();
     const int tiles_x = (cam.w + 7) >> 3;
     const float4 miss = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
@@ -374,7 +416,8 @@ __global__ void __launch_bounds__(128) march_persistent_kernel(MapDev m, Cam cam
                     y = (t / tiles_x) * 4 + (l >> 3);
                     if (x < cam.w && y < cam.h) {
                         if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)),
-                                      __ldg(zfar + (y >> 3) * zw + (x >> 3)), x, y, R))
+                                      __ldg(zfar + (y >> 3) * zw + (x >> 3)), __ldg(fnear + (y >> 2) * fw + (x >> 2)),
+                                      x, y, R))
                             active = true;
                         else
                             vmap[(size_t)y * vpitch + x] = miss;
@@ -422,15 +465,15 @@ static void launch_march_persistent(const MapDev &m, int fmt, const Cam &cam, co
     switch (fmt) {
         case YAS_VOXEL_F32:
             march_persistent_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                        vmap_pitch_elems, skip, rb.queue, total);
+                                                                        vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
             break;
         case YAS_VOXEL_F16:
             march_persistent_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                        vmap_pitch_elems, skip, rb.queue, total);
+                                                                        vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
             break;
         default:
             march_persistent_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                        vmap_pitch_elems, skip, rb.queue, total);
+                                                                        vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
             break;
     }
 }
@@ -443,15 +486,15 @@ static void launch_march_tile(const MapDev &m, int fmt, const Cam &cam, const Po
     switch (fmt) {
         case YAS_VOXEL_F32:
             march_kernel<YAS_VOXEL_F32, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                         vmap_pitch_elems, skip);
+                                                                         vmap_pitch_elems, skip, rb.fnear, rb.fw);
             break;
         case YAS_VOXEL_F16:
             march_kernel<YAS_VOXEL_F16, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                         vmap_pitch_elems, skip);
+                                                                         vmap_pitch_elems, skip, rb.fnear, rb.fw);
             break;
         default:
             march_kernel<YAS_VOXEL_S24, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
-                                                                         vmap_pitch_elems, skip);
+                                                                         vmap_pitch_elems, skip, rb.fnear, rb.fw);
             break;
     }
 }

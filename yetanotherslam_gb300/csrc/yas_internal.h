@@ -95,6 +95,8 @@ struct RaycastBuffers {
     float *znear;      // zw*zh
     float *zfar;       // zw*zh
     unsigned *queue;   // next pixel of the persistent march (reset with the z-range)
+    int fw, fh;        // fine near-bound map size: ceil(w/4), ceil(h/4)
+    float *fnear;      // fw*fh: nearest visible block whose projected box covers the 4x4 pixels
 };
 void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBuffers &rb,
                    const int *skip, cudaStream_t s);
