@@ -512,7 +512,8 @@ def run_batched(seed: int = 7, only_pass: bool = False):
     return {"config": dict(cfg, mix=[{"res": f"{p[0]}x{p[1]}", "voxel_m": p[2], "frames": p[3]} for p in plan]),
             "submap_frames": f_tun, "steps": max(p[3] for p in plan), "kernels_per_step": kernels,
             "tuning": {"march_warps_x": tuned.march_warps_x, "integrate_ctas": tuned.integrate_ctas,
-                       "gn_pixels_per_cta": tuned.gn_pixels_per_cta}, "autotune_s": round(tune_s, 2),
+                       "gn_pixels_per_cta": tuned.gn_pixels_per_cta, "gn_per_session": tuned.gn_per_session},
+            "autotune_s": round(tune_s, 2),
             "batched_fps_device": round(t_fps, 1), "batched_fps_wall": round(f_tun / wall_tun, 1),
             "batched_default_fps_device": round(f_def / (ms_def * 1e-3), 1),
             "frame_status_nonzero": bad_tun + bad_def,

@@ -465,9 +465,14 @@ typedef struct yas_batch_tuning {
                             * > 0: one CTA per this many level-0 pixels (1..16 per
                             * session), which fixes each session's summation order, so
                             * its results do not depend on the rest of the batch      */
+    int gn_per_session;    /* 1: each session's GN schedule is its own cooperative
+                            * launch in the session's branch of the graph (sessions
+                            * overlap their halves with other sessions' GN); 0: one
+                            * launch for every session of the step (split only if
+                            * its CTAs exceed what is co-resident); same results    */
 } yas_batch_tuning;
 
-/* Defaults: 2, 1216 (152 x 8), 0. */
+/* Defaults: 2, 1216 (152 x 8), 0, 1. */
 YAS_API int yas_batch_tuning_default(yas_batch_tuning *t);
 YAS_API int yas_batch_create(yas_batch **out, yas_session *const *sessions, int count, void *stream);
 YAS_API int yas_batch_destroy(yas_batch *b);
@@ -488,7 +493,8 @@ YAS_API int yas_batch_kernels_per_step(yas_batch *b, int *out);
  * scratch sessions and runs them through the first `frames` (>= 3) frames of
  * each session: rgb[i] / depth[i] hold that many consecutive frames.  Each
  * knob (GN share, march CTA shape, integration grid) is tried in turn over a
- * few candidate values, the others held, each candidate timed by the median
+ * few candidate values (GN share, GN launches per session or per step, march
+ * CTA shape, integration grid), the others held, each candidate timed by the median
  * device time of its steps.  The fastest value is kept, applied to the batch
  * and written to *out (may be NULL).  The batch's own sessions are not
  * touched. */

@@ -73,16 +73,27 @@ def test_batch_matches_sessions_run_alone(cuda):
             assert dt <= 5e-5 and dr <= 5e-5, (i, f, dt, dr)
 
 
-def test_session_result_is_the_same_alone_and_in_the_mix(cuda):
+@pytest.mark.parametrize("per_session", [0, 1])
+def test_session_result_is_the_same_alone_and_in_the_mix(cuda, per_session):
     # with a fixed GN share per resolution (the proportional default splits the
-    # GPU by the step's mix, so it fixes the summation order per mix instead)
+    # GPU by the step's mix, so it fixes the summation order per mix instead);
+    # one GN launch per step or one per session give the same results
     fixed = batching.default_tuning()
     fixed.gn_pixels_per_cta = 32768
+    fixed.gn_per_session = per_session
     _, _, mixed = _run_batch(MIX, fixed)
     for i in (0, 2):
         _, _, alone = _run_batch([MIX[i]], fixed)
         for A, B in zip(mixed[i], alone[0]):
             assert np.array_equal(A, B)
+    if per_session:
+        other = batching.default_tuning()
+        other.gn_pixels_per_cta = 32768
+        other.gn_per_session = 0
+        _, _, one_launch = _run_batch(MIX, other)
+        for i in range(len(MIX)):
+            for A, B in zip(mixed[i], one_launch[i]):
+                assert np.array_equal(A, B)
 
 
 def test_launch_shapes_do_not_change_results(cuda):
@@ -113,9 +124,10 @@ def test_autotune_picks_a_candidate_and_leaves_sessions_untouched(cuda):
     assert t.gn_pixels_per_cta in (0, 16384, 32768, 65536)
     assert t.march_warps_x in (0, 1, 2, 4)
     assert t.integrate_ctas in (152 * 4, 152 * 8, 152 * 16)
+    assert t.gn_per_session in (0, 1)
     got = b.tuning
-    assert (got.gn_pixels_per_cta, got.march_warps_x, got.integrate_ctas) == (
-        t.gn_pixels_per_cta, t.march_warps_x, t.integrate_ctas)
+    assert (got.gn_pixels_per_cta, got.march_warps_x, got.integrate_ctas, got.gn_per_session) == (
+        t.gn_pixels_per_cta, t.march_warps_x, t.integrate_ctas, t.gn_per_session)
     for s in ss:
         assert s.map().Empty()
     # the tuned batch steps as a fresh batch with that tuning

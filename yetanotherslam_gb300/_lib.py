@@ -58,7 +58,8 @@ class ServerConfig(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("march_warps_x", C.c_int), ("integrate_ctas", C.c_int), ("gn_pixels_per_cta", C.c_int)]
+    _fields_ = [("march_warps_x", C.c_int), ("integrate_ctas", C.c_int), ("gn_pixels_per_cta", C.c_int),
+                ("gn_per_session", C.c_int)]
 
 
 class ServedResult(C.Structure):

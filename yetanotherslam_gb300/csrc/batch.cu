@@ -73,7 +73,8 @@ static LaunchShape shape_of(const yas_batch_tuning &t) {
 static bool tuning_valid(const yas_batch_tuning &t) {
     return (t.march_warps_x == 0 || t.march_warps_x == 1 || t.march_warps_x == 2 || t.march_warps_x == 4) &&
            t.integrate_ctas > 0 &&
-           t.integrate_ctas <= (1 << 20) && (t.gn_pixels_per_cta == 0 || t.gn_pixels_per_cta >= 1024);
+           t.integrate_ctas <= (1 << 20) && (t.gn_pixels_per_cta == 0 || t.gn_pixels_per_cta >= 1024) &&
+           (t.gn_per_session == 0 || t.gn_per_session == 1);
 }
 
 static void free_cached(CachedStep &c) {
@@ -219,6 +220,20 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
     std::vector<GNGroup> groups;
     YAS_TRY(plan_gn(b, key, items, cta_item, groups));
     out.key = key;
+    const bool chains = b->tuning.gn_per_session != 0;
+    std::vector<int> item_of(b->s.size(), -1);  // chains: session -> its descriptor
+    if (chains && !items.empty()) {
+        // every descriptor becomes a launch of its own: CTA numbering from 0,
+        // and one all-zero CTA -> item map shared by the launches
+        int most = 0;
+        for (GNBatchItem &it : items) {
+            it.cta0 = 0;
+            most = std::max(most, it.nctas);
+        }
+        cta_item.assign((size_t)most, 0);
+        for (size_t i = 0, k = 0; i < b->s.size(); ++i)
+            if (key[i] >= kTrack0) item_of[i] = (int)k++;
+    }
     if (!items.empty()) {
         if (cudaMalloc(&out.d_items, items.size() * sizeof(GNBatchItem)) != cudaSuccess ||
             cudaMalloc(&out.d_map, cta_item.size() * sizeof(unsigned short)) != cudaSuccess) {
@@ -239,27 +254,36 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
         cudaStream_t st = session_stream(s);
         err = cudaStreamWaitEvent(st, b->ev_fork, 0);
         if (err != cudaSuccess) break;
-        if (key[i] == kFirst)
+        if (key[i] == kFirst) {
             session_enqueue_first(s);
-        else
+        } else {
             session_enqueue_pre(s);
-        err = cudaEventRecord(b->ev_pre[i], st);
+            if (chains) {  // the session's own GN launch, then its second half
+                const int k = item_of[i];
+                err = launch_gn_batch(out.d_items + k, out.d_map, items[(size_t)k].nctas, st,
+                                      gn_batch_pix(&items[(size_t)k], 1));
+                if (err == cudaSuccess) session_enqueue_post(s);
+            }
+        }
+        if (err == cudaSuccess) err = cudaEventRecord(chains && key[i] >= kTrack0 ? b->ev_post[i] : b->ev_pre[i], st);
     }
-    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i)
-        if (key[i] >= kTrack0) err = cudaStreamWaitEvent(b->stream, b->ev_pre[i], 0);
-    for (const GNGroup &g : groups) {
-        if (err != cudaSuccess) break;
-        err = launch_gn_batch(out.d_items + g.item0, out.d_map + g.cta0, g.nctas, b->stream, g.pix);
-    }
-    if (err == cudaSuccess && !groups.empty()) err = cudaEventRecord(b->ev_gn, b->stream);
-    for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
-        if (key[i] < kTrack0) continue;
-        yas_session *s = b->s[i];
-        cudaStream_t st = session_stream(s);
-        err = cudaStreamWaitEvent(st, b->ev_gn, 0);
-        if (err != cudaSuccess) break;
-        session_enqueue_post(s);
-        err = cudaEventRecord(b->ev_post[i], st);
+    if (!chains) {
+        for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i)
+            if (key[i] >= kTrack0) err = cudaStreamWaitEvent(b->stream, b->ev_pre[i], 0);
+        for (const GNGroup &g : groups) {
+            if (err != cudaSuccess) break;
+            err = launch_gn_batch(out.d_items + g.item0, out.d_map + g.cta0, g.nctas, b->stream, g.pix);
+        }
+        if (err == cudaSuccess && !groups.empty()) err = cudaEventRecord(b->ev_gn, b->stream);
+        for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
+            if (key[i] < kTrack0) continue;
+            yas_session *s = b->s[i];
+            cudaStream_t st = session_stream(s);
+            err = cudaStreamWaitEvent(st, b->ev_gn, 0);
+            if (err != cudaSuccess) break;
+            session_enqueue_post(s);
+            err = cudaEventRecord(b->ev_post[i], st);
+        }
     }
     for (size_t i = 0; i < b->s.size() && err == cudaSuccess; ++i) {
         if (key[i] == kIdle) continue;
@@ -319,6 +343,7 @@ YAS_API int yas_batch_tuning_default(yas_batch_tuning *t) {
     t->march_warps_x = 2;
     t->integrate_ctas = 152 * 8;
     t->gn_pixels_per_cta = 0;
+    t->gn_per_session = 1;
     return YAS_OK;
 }
 
@@ -492,15 +517,19 @@ YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const ui
     yas_batch_tuning best = b->tuning;
     float best_ms = 0.0f;
     if (st == YAS_OK) st = measure(best, &best_ms);
-    // coordinate descent, one pass: GN share, march CTA shape, integration grid
+    // coordinate descent, one pass: GN share, GN launches, march CTA shape, integration grid
     const int gn_c[4] = {0, 16384, 32768, 65536};
     const int mw_c[4] = {0, 1, 2, 4};
     const int ig_c[4] = {152 * 4, 152 * 8, 152 * 16, 152 * 8};
-    for (int knob = 0; knob < 3 && st == YAS_OK; ++knob) {
+    const int ps_c[4] = {0, 1, 1, 1};
+    for (int knob = 0; knob < 4 && st == YAS_OK; ++knob) {
         for (int v = 0; v < 4 && st == YAS_OK; ++v) {
             yas_batch_tuning t = best;
-            int *field = knob == 0 ? &t.gn_pixels_per_cta : (knob == 1 ? &t.march_warps_x : &t.integrate_ctas);
-            const int value = knob == 0 ? gn_c[v] : (knob == 1 ? mw_c[v] : ig_c[v]);
+            int *field = knob == 0   ? &t.gn_pixels_per_cta
+                         : knob == 1 ? &t.gn_per_session
+                         : knob == 2 ? &t.march_warps_x
+                                     : &t.integrate_ctas;
+            const int value = knob == 0 ? gn_c[v] : knob == 1 ? ps_c[v] : knob == 2 ? mw_c[v] : ig_c[v];
             if (*field == value) continue;
             *field = value;
             float m = 0.0f;
