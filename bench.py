@@ -3,7 +3,7 @@
 Workload (the BASELINE metric's configuration): 640x480 RGB-D frames of the
 seeded synthetic scene (box room, 20 spheres, 10 cuboids, sigma = 1.5 mm z^2
 depth noise, 1 % dropout), 5 mm voxels, truncation 3 voxels, 2^21 hash
-slots, FP16 TSDF + u16 weight, 3-level RGB+ICP pyramid with {10,5,3} GN
+slots, FP16 TSDF + u8 weight (rounding residual kept), 3-level RGB+ICP pyramid with {10,5,3} GN
 iterations.  A step is one frame of the sequence through the whole dense
 path: image and depth pyramids, raycast of the map at the previous pose,
 model pyramid, 18 Gauss-Newton iterations with the device-side FP64 solve,
@@ -41,7 +41,7 @@ METRIC = "frames/sec tracking+fusion @640x480/5mm; p50/p99 frame latency at 32 s
 WORKLOAD = {
     "workload": "single-session tracking+fusion, 640x480, 5 mm voxels, seeded synthetic RGB-D sequence",
     "width": 640, "height": 480, "voxel_m": 0.005, "trunc_m": 0.015, "hash_slots": 1 << 21,
-    "max_blocks": 1 << 18, "tsdf": "fp16+u16", "pyramid_levels": 3, "gn_iterations": [10, 5, 3],
+    "max_blocks": 1 << 18, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)", "pyramid_levels": 3, "gn_iterations": [10, 5, 3],
     "mode": "rgb+icp", "scene_seed": 1,
 }
 
@@ -295,7 +295,7 @@ def run_gpu(args):
 
 SERVED = {"sessions": 32, "rate_hz": 30.0, "seconds": 3.0, "resolutions": [[640, 480], [320, 240]],
           "voxel_m": 0.005, "trunc_m": 0.015, "hash_slots": {"640x480": 1 << 21, "320x240": 1 << 20},
-          "max_blocks": 1 << 17, "tsdf": "fp16+u16", "rendered_frames": 30, "saturate_seconds": 1.5}
+          "max_blocks": 1 << 17, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)", "rendered_frames": 30, "saturate_seconds": 1.5}
 
 
 def _pingpong(k: int, n: int) -> int:
@@ -414,7 +414,7 @@ def run_served(seed: int = 100):
 
 
 BATCHED = {"submaps": 16, "resolutions": [[320, 240], [480, 360], [640, 480]], "voxel_m": [0.005, 0.008],
-           "frames": [5, 60], "hash_slots": 1 << 20, "max_blocks": 1 << 17, "tsdf": "fp16+u16",
+           "frames": [5, 60], "hash_slots": 1 << 20, "max_blocks": 1 << 17, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)",
            "calibration_frames": 4}
 
 
@@ -523,7 +523,7 @@ def run_batched(seed: int = 7, only_pass: bool = False):
 
 
 LARGE = {"frames": 2000, "width": 1280, "height": 720, "voxel_m": 0.004, "trunc_m": 0.012, "hash_slots": 1 << 23,
-         "max_blocks": 1 << 21, "tsdf": "fp16+u16", "seed": 5, "correction_frame": 1800,
+         "max_blocks": 1 << 21, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)", "seed": 5, "correction_frame": 1800,
          "scene": "four rooms in a 12 x 4 x 12 m box (interior walls with doorways), 80 objects, "
                   "a closed loop of radius 4.5 m over the 2000 frames",
          "mesher_max_triangles": 40_000_000}

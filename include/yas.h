@@ -67,7 +67,8 @@ typedef struct yas_pose {
  * (running weighted average, weight + 1 capped at 255). */
 enum yas_voxel_format {
     YAS_VOXEL_F32 = 0, /* float sdf + float weight, 8 B/voxel              */
-    YAS_VOXEL_F16 = 1, /* fp16 sdf + u16 weight, 4 B/voxel                 */
+    YAS_VOXEL_F16 = 1, /* fp16 sdf + u8 weight, 4 B/voxel; the spare byte  *
+                        * keeps the fp16 rounding residual (1/256 ulp)    */
     YAS_VOXEL_S24 = 2  /* 24-bit fixed-point sdf (2^-22 step) + u8 weight, 4 B */
 };
 
@@ -151,7 +152,7 @@ YAS_API int yas_map_device_bytes(yas_map *map, size_t *out_bytes);
 YAS_API int yas_map_reserve(yas_map *map, int hash_slots, int max_blocks);
 /* MapStruct::SaveToFile / ReadFromFile (VoxelMap.h:65-66; empty stubs at
  * VoxelMap.cu:886-893): a binary submap file (144-byte header: magic
- * "YASSUBM1", version 1, voxel format, voxel size, truncation, depth gates,
+ * "YASSUBM1", version 2, voxel format, voxel size, truncation, depth gates,
  * weight cap, capacities, block count, pose; then int32 block coordinates; then
  * the voxels in the map's storage format).  Loading replaces the map's
  * contents and pose, grows it if needed, and needs the same voxel format and

@@ -6,7 +6,7 @@ with {10, 5, 3} iterations, marching cubes every 50 frames.  Four GPU
 sessions run the same frames:
 
   f32_comp   FP32 TSDF (float sdf + float weight), compensated FP32 sums
-  f16_comp   FP16 TSDF (half sdf + u16 weight),   compensated FP32 sums
+  f16_comp   FP16 TSDF (half sdf, its rounding residual, u8 weight), compensated FP32 sums
   f32_plain  FP32 TSDF,                            plain FP32 sums
   f16_plain  FP16 TSDF,                            plain FP32 sums
 

@@ -128,16 +128,41 @@ struct VoxelIO<YAS_VOXEL_F32> {
     __device__ __forceinline__ static T make(float s, int w) { return make_float2(s, (float)w); }
 };
 
+// FP16 value + u8 weight, with the FP16 rounding residual in the word's spare
+// byte: bits 0..15 the half h, bits 16..23 a signed residual q in 1/256 of h's
+// ulp, bits 24..31 the weight.  The value is h + q ulp(h) / 256: 19 significant
+// bits, exact in FP32, so every write keeps 8 more bits than the half alone
+// and the running average's rounding stays ~256x smaller.
+// ulp(h) / 256 and its inverse, powers of two read off the half's exponent
+// field e (ulp = 2^(e-25), or 2^-24 for subnormals), so scaling by them is exact.
+__device__ __forceinline__ unsigned half_exp(unsigned short hb) {
+    const unsigned e = (hb >> 10) & 0x1fu;
+    return e ? e : 1u;
+}
+__device__ __forceinline__ float residual_scale(unsigned short hb) {  // 2^(e-33)
+    return __int_as_float((int)((half_exp(hb) + 94u) << 23));
+}
+__device__ __forceinline__ float residual_inv_scale(unsigned short hb) {  // 2^(33-e)
+    return __int_as_float((int)((160u - half_exp(hb)) << 23));
+}
+
 template <>
 struct VoxelIO<YAS_VOXEL_F16> {
     typedef unsigned T;
     static constexpr int kBytes = 4;
     __device__ __forceinline__ static float sdf(T v) {
-        return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+        const unsigned short hb = (unsigned short)(v & 0xffffu);
+        const int q = (int)(signed char)((v >> 16) & 0xffu);
+        // exact: q * 2^(e-33) has 8 bits, and the sum fits 19 significant bits
+        return __fmaf_rn((float)q, residual_scale(hb), __half2float(__ushort_as_half(hb)));
     }
-    __device__ __forceinline__ static int wt(T v) { return (int)(v >> 16); }
+    __device__ __forceinline__ static int wt(T v) { return (int)(v >> 24); }
     __device__ __forceinline__ static T make(float s, int w) {
-        return (unsigned)__half_as_ushort(__float2half_rn(s)) | ((unsigned)w << 16);
+        const unsigned short hb = __half_as_ushort(__float2half_rn(s));
+        const float r = __fsub_rn(s, __half2float(__ushort_as_half(hb)));  // exact: |r| <= ulp / 2
+        int q = __float2int_rn(__fmul_rn(r, residual_inv_scale(hb)));
+        q = max(-128, min(127, q));
+        return (unsigned)hb | (((unsigned)q & 0xffu) << 16) | ((unsigned)min(w, 255) << 24);
     }
 };
 
