@@ -222,6 +222,10 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
     out.key = key;
     const bool chains = b->tuning.gn_per_session != 0;
     std::vector<int> item_of(b->s.size(), -1);  // chains: session -> its descriptor
+    std::vector<int> group_of(items.size(), 0);  // chains: descriptor -> its group
+    for (size_t g = 0; g < groups.size(); ++g)
+        for (int k = 0; k < groups[g].nitems; ++k) group_of[(size_t)(groups[g].item0 + k)] = (int)g;
+    std::vector<size_t> session_of(items.size(), 0);
     if (chains && !items.empty()) {
         // every descriptor becomes a launch of its own: CTA numbering from 0,
         // and one all-zero CTA -> item map shared by the launches
@@ -232,7 +236,10 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
         }
         cta_item.assign((size_t)most, 0);
         for (size_t i = 0, k = 0; i < b->s.size(); ++i)
-            if (key[i] >= kTrack0) item_of[i] = (int)k++;
+            if (key[i] >= kTrack0) {
+                session_of[k] = i;
+                item_of[i] = (int)k++;
+            }
     }
     if (!items.empty()) {
         if (cudaMalloc(&out.d_items, items.size() * sizeof(GNBatchItem)) != cudaSuccess ||
@@ -260,8 +267,17 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
             session_enqueue_pre(s);
             if (chains) {  // the session's own GN launch, then its second half
                 const int k = item_of[i];
-                err = launch_gn_batch(out.d_items + k, out.d_map, items[(size_t)k].nctas, st,
-                                      gn_batch_pix(&items[(size_t)k], 1));
+                // the CTAs of one group fit the GPU together; a later group's
+                // launches wait until the previous group's sessions are done
+                const int g = group_of[(size_t)k];
+                if (g > 0) {
+                    const GNGroup &pg = groups[(size_t)(g - 1)];
+                    for (int j = 0; j < pg.nitems && err == cudaSuccess; ++j)
+                        err = cudaStreamWaitEvent(st, b->ev_post[session_of[(size_t)(pg.item0 + j)]], 0);
+                }
+                if (err == cudaSuccess)
+                    err = launch_gn_batch(out.d_items + k, out.d_map, items[(size_t)k].nctas, st,
+                                          gn_batch_pix(&items[(size_t)k], 1));
                 if (err == cudaSuccess) session_enqueue_post(s);
             }
         }
