@@ -249,7 +249,7 @@ def run_gpu(args):
 
     # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
     cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
-    served = run_served(100 + 1000 * rank) if args.served else None
+    served = run_served(100 + 1000 * rank, args.served_gn) if args.served else None
     batched = run_batched(7 + 1000 * rank) if args.batched else None
     large = run_large(args.large_frames) if args.large else None
 
@@ -305,7 +305,7 @@ def _pingpong(k: int, n: int) -> int:
     return k if k < n else period - k
 
 
-def run_served(seed: int = 100):
+def run_served(seed: int = 100, gn_per_session: bool | None = None):
     """C4: 32 concurrent sessions (half 640x480, half 320x240, distinct seeded scenes), Poisson
     arrivals at 30 Hz per session, through the request server; then the same sessions saturated
     (every session resubmits as soon as its ring has room); then the plain FP32 per-frame form
@@ -321,7 +321,8 @@ def run_served(seed: int = 100):
     for i in range(cfg["sessions"]):
         W, H = cfg["resolutions"][i % 2]
         sessions.append((W, H, make_frames(n_r, W, H, seed + i)))
-    srv = serving.Server(max_sessions=cfg["sessions"], hbm_reserve_bytes=8 << 30, ring_frames=8)
+    srv = serving.Server(max_sessions=cfg["sessions"], hbm_reserve_bytes=8 << 30, ring_frames=8,
+                         gn_per_session=gn_per_session)
     sids = []
     for W, H, _ in sessions:
         sids.append(srv.open(W, H, synth.intrinsics(W, H), hash_slots=cfg["hash_slots"][f"{W}x{H}"],
@@ -405,7 +406,8 @@ def run_served(seed: int = 100):
     plain_fps = n_plain / (time.perf_counter() - t0)
     for p, _ in plains:
         p.close()
-    return {"config": {k: v for k, v in cfg.items()}, "poisson": poisson,
+    gn_mode = "per session" if gn_per_session in (None, True, 1) else "gathered into batched launches"
+    return {"config": dict(cfg, gauss_newton=gn_mode), "poisson": poisson,
             "saturated": {"frames": int(sat["frames"]), "fps": round(sat["fps"], 1),
                           "p50_ms": round(sat["p50_ms"], 3), "p99_ms": round(sat["p99_ms"], 3),
                           "mean_batch": round(sat["mean_batch"], 2)},
@@ -697,6 +699,8 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=4)
     ap.add_argument("--cpu-frames", type=int, default=8)
     ap.add_argument("--served", type=int, default=1, help="1: also measure 32 served sessions (C4)")
+    ap.add_argument("--served-gn", type=lambda v: bool(int(v)), default=None,
+                    help="served sessions: 1 = a GN launch per session (the server's default), 0 = gathered")
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
     ap.add_argument("--large", type=int, default=0, help="1: also run the 2000-frame 1280x720 large map (C5)")
     ap.add_argument("--large-frames", type=int, default=2000)
@@ -706,7 +710,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.leg:
-        fn = {"served": lambda: run_served(100), "batched": lambda: run_batched(7),
+        fn = {"served": lambda: run_served(100, args.served_gn), "batched": lambda: run_batched(7),
               "batched-pass": lambda: run_batched(7, only_pass=True),
               "large": lambda: run_large(args.large_frames)}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn()}))

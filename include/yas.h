@@ -152,7 +152,7 @@ YAS_API int yas_map_device_bytes(yas_map *map, size_t *out_bytes);
 YAS_API int yas_map_reserve(yas_map *map, int hash_slots, int max_blocks);
 /* MapStruct::SaveToFile / ReadFromFile (VoxelMap.h:65-66; empty stubs at
  * VoxelMap.cu:886-893): a binary submap file (144-byte header: magic
- * "YASSUBM1", version 2, voxel format, voxel size, truncation, depth gates,
+ * "YASSUBM1", version 3, voxel format, voxel size, truncation, depth gates,
  * weight cap, capacities, block count, pose; then int32 block coordinates; then
  * the voxels in the map's storage format).  Loading replaces the map's
  * contents and pose, grows it if needed, and needs the same voxel format and
@@ -517,6 +517,10 @@ typedef struct yas_server_config {
     int max_sessions;         /* live sessions at most                               */
     size_t hbm_reserve_bytes; /* admission: free HBM - session footprint >= this    */
     int ring_frames;          /* queued frames per session (pinned input ring)      */
+    int gn_per_session;       /* 1: a taken frame runs its own Gauss-Newton launch  *
+                               * (a fixed CTA share) on its session's stream at   *
+                               * once; 0: sessions whose first half is queued     *
+                               * gather into one batched launch                   */
 } yas_server_config;
 
 typedef struct yas_served_result {
@@ -535,7 +539,8 @@ typedef struct yas_server_stats {
     double fps;        /* completed frames / (last completion - first submission) */
 } yas_server_stats;
 
-/* Defaults: 64 sessions, 4 GiB reserve, 4 queued frames per session. */
+/* Defaults: 64 sessions, 4 GiB reserve, 4 queued frames per session, GN per
+ * session. */
 YAS_API int yas_server_config_default(yas_server_config *cfg);
 /* Starts the server's worker thread on the current device. */
 YAS_API int yas_server_create(yas_server **out, const yas_server_config *cfg);

@@ -3,7 +3,8 @@
 Bars:
   * a session's poses are bit-identical alone in the server and in a mix with
     other sessions of other resolutions (its work does not depend on its
-    batch: fixed CTA share, own rows, own state);
+    batch: fixed CTA share, own rows, own state), with a GN launch per session
+    (the default) and with waiting sessions gathered into one batched launch;
   * served poses agree with the same sequence run through a standalone
     session within 1e-5 m / rad (same arithmetic per pixel, another fold
     order of the partial sums);
@@ -27,8 +28,8 @@ pytestmark = pytest.mark.gpu
 MAP = dict(hash_slots=1 << 18, max_blocks=1 << 15, voxel_size=0.008, voxel_format=rf.VOXEL_F16)
 
 
-def _serve_alone(seq, W, H):
-    srv = serving.Server(hbm_reserve_bytes=1 << 30)
+def _serve_alone(seq, W, H, gn_per_session=None):
+    srv = serving.Server(hbm_reserve_bytes=1 << 30, gn_per_session=gn_per_session)
     sid = srv.open(W, H, synth.intrinsics(W, H), **MAP)
     poses = []
     for rgb, d16, _, _ in seq:
@@ -41,17 +42,19 @@ def _serve_alone(seq, W, H):
     return poses
 
 
-def test_served_sessions_same_alone_and_in_mix(cuda):
-    """Eight sessions of three resolutions submit concurrently (so batches of
-    several sessions form and GN dispatch is deferred while one runs); every
-    session's poses equal, bit for bit, its poses served alone."""
+@pytest.mark.parametrize("per_session", [True, False])
+def test_served_sessions_same_alone_and_in_mix(cuda, per_session):
+    """Eight sessions of three resolutions submit concurrently (their frames
+    overlap on the device; gathered, batches of several sessions form and GN
+    dispatch is deferred while one runs); every session's poses equal, bit for
+    bit, its poses served alone."""
     n = 8
     specs = [(320, 240, 3), (160, 120, 5), (320, 240, 7), (640, 480, 9),
              (160, 120, 11), (640, 480, 13), (320, 240, 15), (160, 120, 17)]
     seqs = [sequence(seed, n, w, h) for w, h, seed in specs]
-    alone = [_serve_alone(seq, w, h) for (w, h, _), seq in zip(specs, seqs)]
+    alone = [_serve_alone(seq, w, h, per_session) for (w, h, _), seq in zip(specs, seqs)]
 
-    srv = serving.Server(hbm_reserve_bytes=1 << 30)
+    srv = serving.Server(hbm_reserve_bytes=1 << 30, gn_per_session=per_session)
     sids = [srv.open(w, h, synth.intrinsics(w, h), **MAP) for w, h, _ in specs]
 
     def feed(s, frames):

@@ -54,7 +54,8 @@ class SessionConfig(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("max_sessions", C.c_int), ("hbm_reserve_bytes", C.c_size_t), ("ring_frames", C.c_int)]
+    _fields_ = [("max_sessions", C.c_int), ("hbm_reserve_bytes", C.c_size_t), ("ring_frames", C.c_int),
+                ("gn_per_session", C.c_int)]
 
 
 class BatchTuning(C.Structure):

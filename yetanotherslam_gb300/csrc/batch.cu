@@ -248,10 +248,14 @@ static int capture_step(yas_batch *b, const std::vector<uint8_t> &key, CachedSte
             free_cached(out);
             return YAS_ERR_OOM;
         }
-        YAS_TRY_CUDA(cudaMemcpy(out.d_items, items.data(), items.size() * sizeof(GNBatchItem),
-                                cudaMemcpyHostToDevice));
-        YAS_TRY_CUDA(cudaMemcpy(out.d_map, cta_item.data(), cta_item.size() * sizeof(unsigned short),
-                                cudaMemcpyHostToDevice));
+        // a synchronous copy from pageable memory may return before its DMA
+        // lands, unordered with the non-blocking step stream: copy on that
+        // stream and wait, before any graph that reads the descriptors runs
+        YAS_TRY_CUDA(cudaMemcpyAsync(out.d_items, items.data(), items.size() * sizeof(GNBatchItem),
+                                     cudaMemcpyHostToDevice, b->stream));
+        YAS_TRY_CUDA(cudaMemcpyAsync(out.d_map, cta_item.data(), cta_item.size() * sizeof(unsigned short),
+                                     cudaMemcpyHostToDevice, b->stream));
+        YAS_TRY_CUDA(cudaStreamSynchronize(b->stream));
     }
     YAS_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t err = cudaEventRecord(b->ev_fork, b->stream);

@@ -546,7 +546,7 @@ static int map_grow(yas_map *m, long long want_slots, long long want_blocks);
 // storage format (8 bytes for F32, 4 for F16 and S24), pool order.
 struct SubmapFileHeader {
     char magic[8];          // "YASSUBM1"
-    uint32_t version;       // 2 (F16 voxels carry their rounding residual)
+    uint32_t version;       // 3 (F16 voxels: half + FP32-bit residual + u8 weight)
     uint32_t voxel_format;  // enum yas_voxel_format
     float voxel_size, trunc_dist, depth_min, depth_max;
     int32_t max_weight, hash_slots, max_blocks;
@@ -574,7 +574,7 @@ YAS_API int yas_map_save(yas_map *m, const char *path) {
     SubmapFileHeader h;
     memset(&h, 0, sizeof(h));
     memcpy(h.magic, kSubmapMagic, 8);
-    h.version = 2;
+    h.version = 3;
     h.voxel_format = (uint32_t)m->cfg.voxel_format;
     h.voxel_size = m->cfg.voxel_size;
     h.trunc_dist = m->cfg.trunc_dist;
@@ -606,7 +606,7 @@ YAS_API int yas_map_load(yas_map *m, const char *path) {
     FILE *f = fopen(path, "rb");
     if (!f) return YAS_ERR_IO;
     SubmapFileHeader h;
-    bool ok = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, kSubmapMagic, 8) == 0 && h.version == 2;
+    bool ok = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, kSubmapMagic, 8) == 0 && h.version == 3;
     const size_t vb = (size_t)kBlockVoxels * (h.voxel_format == YAS_VOXEL_F32 ? 8 : 4);
     std::vector<int32_t> coords;
     std::vector<unsigned char> vox;
@@ -902,7 +902,13 @@ YAS_API int yas_raycaster_create(yas_raycaster **out, int width, int height, con
         yas_raycaster_destroy(rc);
         return YAS_ERR_OOM;
     }
-    cudaMemset(rc->vmap, 0, (size_t)width * height * 16);
+    // the zero fill runs on the legacy stream, which the raycaster's
+    // non-blocking stream does not wait for
+    if (cudaMemset(rc->vmap, 0, (size_t)width * height * 16) != cudaSuccess ||
+        cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) {
+        yas_raycaster_destroy(rc);
+        return YAS_ERR_CUDA;
+    }
     *out = rc;
     return YAS_OK;
 }

@@ -147,6 +147,9 @@ void mesh_tables_upload() {
     cudaMemcpyToSymbol(c_edge_table, tables.edge, sizeof(tables.edge));
     cudaMemcpyToSymbol(c_tri_table, tables.tri, sizeof(tables.tri));
     cudaMemcpyToSymbol(c_tri_count, tables.count, sizeof(tables.count));
+    // the copies run on the legacy stream; the engines launch on
+    // non-blocking streams, which do not wait for it
+    cudaStreamSynchronize(cudaStreamLegacy);
 }
 
 // ---------------------------------------------------------------- staging

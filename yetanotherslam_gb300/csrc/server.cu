@@ -15,6 +15,13 @@
 //      the server's GN stream, every session whose first half is queued joins
 //      one batched launch; the second halves (pose update, fusion, frame
 //      state to the host) follow on the session streams.
+//      With gn_per_session set, a taken frame instead gets its own GN launch
+//      (a one-session batch of a fixed CTA share) and its second half on its
+//      session's stream as soon as its share fits: frames take the GPU in the
+//      order their first halves were launched, and the shares of the GN
+//      launches that may be running never exceed the co-resident CTAs, so
+//      every cooperative grid can be resident at once.  No session waits for
+//      others to gather.
 // Frames that arrive while others are on the GPU start at once and their
 // work overlaps with the running batch; under load the batches grow.  Each session keeps
 // its map, pyramids and buffers device resident; a session is admitted only
@@ -62,6 +69,12 @@ struct ServedSession {
     bool awaiting_gn = false;  // first half launched, GN not yet dispatched
     QueuedFrame cur{};
     cudaEvent_t ev_pre = nullptr, ev_done = nullptr;
+    GNBatchItem *d_own = nullptr;  // gn_per_session: the session's descriptor per frame parity
+    GNBatchItem *h_own = nullptr;  // pinned source of d_own, written once per parity
+    bool own_ready[2] = {false, false};
+    int own_ctas = 0, own_pix = 0;
+    cudaEvent_t ev_gn = nullptr;  // after the session's own GN launch
+    bool gn_running = false;      // its share counts against the co-resident CTAs
     long long submitted = 0, completed = 0;
     bool closing = false;
     bool suspended = false;  // map swapped out to host memory; frames wait in the queue
@@ -106,6 +119,9 @@ struct yas_server {
     int desc_next = 0;
     int capacity = 0;  // co-resident CTAs of the batched launch
     int max_items = 0;
+    unsigned short *d_zero_map = nullptr;  // gn_per_session: every CTA serves item 0
+    std::deque<ServedSession *> own_wait;  // gn_per_session: first halves launched, in order
+    int own_ctas_running = 0;              // shares of the own GN launches not known finished
 };
 
 namespace {
@@ -137,6 +153,10 @@ bool collect_done(yas_server *srv) {
         srv->last_done = now;
         ss->slot_used[ss->cur.slot] = false;
         ss->in_flight = false;
+        if (ss->gn_running) {  // its GN ran before its second half on the same stream
+            ss->gn_running = false;
+            srv->own_ctas_running -= ss->own_ctas;
+        }
         ss->completed++;
         any = true;
     }
@@ -165,6 +185,59 @@ int launch_pre_frame(ServedSession *ss) {
     YAS_TRY_CUDA(cudaEventRecord(ss->ev_pre, session_stream(ss->s)));
     ss->in_flight = true;
     ss->awaiting_gn = true;
+    return YAS_OK;
+}
+
+// CTA share of a session's own GN launch: 16 K pixels of level 0 per CTA.
+constexpr int kOwnPixelsPerCta = 16384;
+
+// gn_per_session: the frame's own GN launch right after its first half, then
+// its second half, all on the session's stream.  The descriptor of each frame
+// parity names the tracker's fixed buffers, so it is built once.
+int own_share(yas_server *srv, ServedSession *ss) {
+    return std::min(srv->capacity, gn_batch_ctas(session_tracker(ss->s), kOwnPixelsPerCta));
+}
+
+int launch_own_gn(yas_server *srv, ServedSession *ss) {
+    yas_tracker *tr = session_tracker(ss->s);
+    const int p = tr->cur;
+    cudaStream_t st = session_stream(ss->s);
+    if (!ss->own_ready[p]) {
+        // the copy is ordered on the session stream before the launch that reads it
+        GNBatchItem &it = ss->h_own[p];
+        gn_batch_item_ctas(tr, 0, own_share(srv, ss), &it);
+        YAS_TRY_CUDA(cudaMemcpyAsync(ss->d_own + p, &it, sizeof(it), cudaMemcpyHostToDevice, st));
+        ss->own_ctas = it.nctas;
+        ss->own_pix = gn_batch_pix(&it, 1);
+        ss->own_ready[p] = true;
+    }
+    YAS_TRY_CUDA(launch_gn_batch(ss->d_own + p, srv->d_zero_map, ss->own_ctas, st, ss->own_pix));
+    YAS_TRY_CUDA(cudaEventRecord(ss->ev_gn, st));
+    ss->gn_running = true;
+    srv->own_ctas_running += ss->own_ctas;
+    YAS_TRY(session_launch_post(ss->s));
+    YAS_TRY_CUDA(cudaEventRecord(ss->ev_done, st));
+    ss->awaiting_gn = false;
+    srv->batches++;
+    srv->batched_frames++;
+    return YAS_OK;
+}
+
+// gn_per_session: frees the shares of finished GN launches, then launches the
+// waiting frames' GN in order while their shares fit.
+int dispatch_own(yas_server *srv, bool &launched) {
+    for (ServedSession *ss : srv->sessions) {
+        if (!ss || !ss->gn_running || cudaEventQuery(ss->ev_gn) == cudaErrorNotReady) continue;
+        ss->gn_running = false;
+        srv->own_ctas_running -= ss->own_ctas;
+    }
+    while (!srv->own_wait.empty()) {
+        ServedSession *ss = srv->own_wait.front();
+        if (srv->own_ctas_running + own_share(srv, ss) > srv->capacity) break;
+        srv->own_wait.pop_front();
+        YAS_TRY(launch_own_gn(srv, ss));
+        launched = true;
+    }
     return YAS_OK;
 }
 
@@ -224,13 +297,15 @@ void worker_main(yas_server *srv) {
             if (!ss) continue;
             if (!ss->closing && !ss->suspended && !ss->in_flight && !ss->queue.empty() && st == YAS_OK) {
                 st = session_needs_init(ss->s) ? launch_first(ss) : launch_pre_frame(ss);
+                if (st == YAS_OK && ss->awaiting_gn && srv->cfg.gn_per_session) srv->own_wait.push_back(ss);
                 launched = true;
             }
             busy = busy || ss->in_flight;
         }
+        if (st == YAS_OK && srv->cfg.gn_per_session) st = dispatch_own(srv, launched);
         // the waiting sessions form the next GN batch once fewer than two
         // batches are on the GN stream (while one runs, the next gathers)
-        if (st == YAS_OK && pending_gn(srv) < 2) {
+        if (st == YAS_OK && !srv->cfg.gn_per_session && pending_gn(srv) < 2) {
             batch.clear();
             int ctas = 0;
             for (ServedSession *ss : srv->sessions) {
@@ -272,6 +347,7 @@ YAS_API int yas_server_config_default(yas_server_config *cfg) {
     cfg->max_sessions = 64;
     cfg->hbm_reserve_bytes = (size_t)4 << 30;
     cfg->ring_frames = 4;
+    cfg->gn_per_session = 1;
     return YAS_OK;
 }
 
@@ -290,6 +366,10 @@ YAS_API int yas_server_create(yas_server **out, const yas_server_config *cfg) {
              cudaMallocHost(&srv->h_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
              cudaMalloc(&srv->d_map[k], srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
              cudaEventCreateWithFlags(&srv->gn_done[k], cudaEventDisableTiming) == cudaSuccess;
+    // zeroed before any session stream can read it
+    ok = ok && cudaMalloc(&srv->d_zero_map, srv->capacity * sizeof(unsigned short)) == cudaSuccess &&
+         cudaMemsetAsync(srv->d_zero_map, 0, srv->capacity * sizeof(unsigned short), srv->gn_stream) == cudaSuccess &&
+         cudaStreamSynchronize(srv->gn_stream) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         const int code = srv->capacity <= 0 ? YAS_ERR_STATE : YAS_ERR_OOM;
@@ -326,7 +406,10 @@ YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *c
         (cudaMallocHost(&ss->rgb, ss->ring * n * 3) != cudaSuccess ||
          cudaMallocHost(&ss->depth, ss->ring * n * 2) != cudaSuccess ||
          cudaEventCreateWithFlags(&ss->ev_pre, cudaEventDisableTiming) != cudaSuccess ||
-         cudaEventCreateWithFlags(&ss->ev_done, cudaEventDisableTiming) != cudaSuccess)) {
+         cudaEventCreateWithFlags(&ss->ev_done, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&ss->ev_gn, cudaEventDisableTiming) != cudaSuccess ||
+         cudaMalloc(&ss->d_own, 2 * sizeof(GNBatchItem)) != cudaSuccess ||
+         cudaMallocHost(&ss->h_own, 2 * sizeof(GNBatchItem)) != cudaSuccess)) {
         cudaGetLastError();
         st = YAS_ERR_OOM;
     }
@@ -336,6 +419,9 @@ YAS_API int yas_server_open_session(yas_server *srv, const yas_session_config *c
         if (ss->depth) cudaFreeHost(ss->depth);
         if (ss->ev_pre) cudaEventDestroy(ss->ev_pre);
         if (ss->ev_done) cudaEventDestroy(ss->ev_done);
+        if (ss->ev_gn) cudaEventDestroy(ss->ev_gn);
+        if (ss->d_own) cudaFree(ss->d_own);
+        if (ss->h_own) cudaFreeHost(ss->h_own);
         delete ss;
         return st;
     }
@@ -412,6 +498,9 @@ YAS_API int yas_server_close_session(yas_server *srv, int id) {
     cudaFreeHost(ss->depth);
     cudaEventDestroy(ss->ev_pre);
     cudaEventDestroy(ss->ev_done);
+    cudaEventDestroy(ss->ev_gn);
+    cudaFree(ss->d_own);
+    cudaFreeHost(ss->h_own);
     delete ss;
     return YAS_OK;
 }
@@ -522,6 +611,9 @@ YAS_API int yas_server_destroy(yas_server *srv) {
         cudaFreeHost(ss->depth);
         cudaEventDestroy(ss->ev_pre);
         cudaEventDestroy(ss->ev_done);
+        cudaEventDestroy(ss->ev_gn);
+        cudaFree(ss->d_own);
+        cudaFreeHost(ss->h_own);
         delete ss;
     }
     if (srv->gn_stream) cudaStreamSynchronize(srv->gn_stream);
@@ -532,6 +624,7 @@ YAS_API int yas_server_destroy(yas_server *srv) {
         if (srv->d_map[k]) cudaFree(srv->d_map[k]);
         if (srv->gn_done[k]) cudaEventDestroy(srv->gn_done[k]);
     }
+    if (srv->d_zero_map) cudaFree(srv->d_zero_map);
     if (srv->gn_stream) cudaStreamDestroy(srv->gn_stream);
     delete srv;
     return YAS_OK;

@@ -1186,6 +1186,9 @@ int tracker_alloc(yas_tracker *tr) {
         return YAS_ERR_OOM;
     }
     memset(tr->state_host, 0, sizeof(GNState));
+    // the zero fills ran on the legacy stream, which the tracker's
+    // non-blocking streams do not wait for
+    if (cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) return YAS_ERR_CUDA;
     return YAS_OK;
 }
 

@@ -129,39 +129,30 @@ struct VoxelIO<YAS_VOXEL_F32> {
 };
 
 // FP16 value + u8 weight, with the FP16 rounding residual in the word's spare
-// byte: bits 0..15 the half h, bits 16..23 a signed residual q in 1/256 of h's
-// ulp, bits 24..31 the weight.  The value is h + q ulp(h) / 256: 19 significant
-// bits, exact in FP32, so every write keeps 8 more bits than the half alone
-// and the running average's rounding stays ~256x smaller.
-// ulp(h) / 256 and its inverse, powers of two read off the half's exponent
-// field e (ulp = 2^(e-25), or 2^-24 for subnormals), so scaling by them is exact.
-__device__ __forceinline__ unsigned half_exp(unsigned short hb) {
-    const unsigned e = (hb >> 10) & 0x1fu;
-    return e ? e : 1u;
-}
-__device__ __forceinline__ float residual_scale(unsigned short hb) {  // 2^(e-33)
-    return __int_as_float((int)((half_exp(hb) + 94u) << 23));
-}
-__device__ __forceinline__ float residual_inv_scale(unsigned short hb) {  // 2^(33-e)
-    return __int_as_float((int)((160u - half_exp(hb)) << 23));
-}
-
+// byte: bits 0..15 the half h, bits 16..23 a signed residual q, bits 24..31 the
+// weight.  The value's FP32 bit pattern is h's (converted exactly) plus 32 q:
+// q counts 2^-18 of h's binade, 1/256 of the half's ulp, on the magnitude.  In
+// the half's normal range a write therefore keeps s rounded to 18 mantissa
+// bits (8 more than the half alone), so the running average's rounding stays
+// ~256x smaller; a read is one conversion, one byte extract and one add.
 template <>
 struct VoxelIO<YAS_VOXEL_F16> {
     typedef unsigned T;
     static constexpr int kBytes = 4;
     __device__ __forceinline__ static float sdf(T v) {
-        const unsigned short hb = (unsigned short)(v & 0xffffu);
-        const int q = (int)(signed char)((v >> 16) & 0xffu);
-        // exact: q * 2^(e-33) has 8 bits, and the sum fits 19 significant bits
-        return __fmaf_rn((float)q, residual_scale(hb), __half2float(__ushort_as_half(hb)));
+        const float h = __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+        const int q = (int)(v << 8) >> 24;
+        return __int_as_float(__float_as_int(h) + q * 32);
     }
     __device__ __forceinline__ static int wt(T v) { return (int)(v >> 24); }
     __device__ __forceinline__ static T make(float s, int w) {
         const unsigned short hb = __half_as_ushort(__float2half_rn(s));
-        const float r = __fsub_rn(s, __half2float(__ushort_as_half(hb)));  // exact: |r| <= ulp / 2
-        int q = __float2int_rn(__fmul_rn(r, residual_inv_scale(hb)));
-        q = max(-128, min(127, q));
+        int q = 0;
+        if (hb & 0x7fffu) {  // h and s share the sign; d = |s| - |h| in FP32 bit units
+            const int d = (__float_as_int(s) & 0x7fffffff) -
+                          (__float_as_int(__half2float(__ushort_as_half(hb))) & 0x7fffffff);
+            q = max(-128, min(127, (d + 16) >> 5));
+        }
         return (unsigned)hb | (((unsigned)q & 0xffu) << 16) | ((unsigned)min(w, 255) << 24);
     }
 };

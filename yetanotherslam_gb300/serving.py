@@ -2,6 +2,9 @@
 
 Frames of many sessions are submitted as they arrive; the server batches them
 continuously on the GPU and returns per-frame results with their latency.
+``gn_per_session`` (the default) gives every taken frame its own Gauss-Newton
+launch on its session's stream; 0 gathers the waiting sessions into one
+batched launch.
 """
 from __future__ import annotations
 
@@ -14,12 +17,15 @@ from .rgbdfusion import session_config
 
 
 class Server:
-    def __init__(self, max_sessions: int = 64, hbm_reserve_bytes: int = 4 << 30, ring_frames: int = 4):
+    def __init__(self, max_sessions: int = 64, hbm_reserve_bytes: int = 4 << 30, ring_frames: int = 4,
+                 gn_per_session: bool | None = None):
         cfg = L.ServerConfig()
         L.call("yas_server_config_default", C.byref(cfg))
         cfg.max_sessions = max_sessions
         cfg.hbm_reserve_bytes = hbm_reserve_bytes
         cfg.ring_frames = ring_frames
+        if gn_per_session is not None:
+            cfg.gn_per_session = int(bool(gn_per_session))
         self.handle = C.c_void_p()
         L.call("yas_server_create", C.byref(self.handle), C.byref(cfg))
         self._sizes: dict[int, tuple[int, int]] = {}
