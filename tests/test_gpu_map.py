@@ -179,6 +179,57 @@ def test_export_import_and_hibernate_roundtrip(cuda):
     assert np.array_equal(sa, sb) and np.array_equal(wa, wb)
 
 
+def _f16_word_model(s, w):
+    """The FP16 voxel word as numpy computes it: the half (round to nearest
+    even), a residual q of 1/256 of the half's ulp added to the half's FP32 bit
+    pattern (q = 0 for a zero half; q = 128 at a normal half becomes -128 at the
+    next half up in magnitude, 2^13 bit units further), the weight capped at 255."""
+    s = s.astype(np.float32)
+    h = s.astype(np.float16).astype(np.float32)
+    hb = h.view(np.int32).astype(np.int64)
+    d = (s.view(np.int32) & 0x7FFFFFFF).astype(np.int64) - (hb & 0x7FFFFFFF)
+    q = (d + 16) >> 5
+    up = (q > 127) & (np.abs(h) >= 2.0 ** -14)
+    hb[up] += 8192
+    q[up] -= 256
+    q = np.clip(q, -128, 127)
+    q[h == 0] = 0
+    v = (hb + 32 * q).astype(np.int32).view(np.float32)
+    return v, np.minimum(w, 255).astype(np.float32)
+
+
+def test_f16_word_keeps_18_mantissa_bits(cuda):
+    """FP16 storage round trip (import, export) of chosen values: bit-exact
+    against the word's numpy model; within 2^-19 relative where the half is
+    normal (|s| >= 2^-14: s rounded to 18 mantissa bits) and 2^-25 absolute
+    below; signs and zeros kept."""
+    rng = np.random.default_rng(77)
+    n_blocks = 64
+    n = n_blocks * 512
+    s = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+    k = n // 8
+    s[:k] = (rng.uniform(-1, 1, k) * 10.0 ** rng.uniform(-9, -4, k)).astype(np.float32)  # half subnormals
+    e = rng.integers(-14, 1, k)  # next to powers of two, both sides
+    s[k:2 * k] = (np.ldexp(1.0, e) * (1.0 + rng.uniform(-2e-3, 2e-3, k)) * rng.choice([-1, 1], k)).astype(np.float32)
+    s[2 * k:2 * k + 6] = [0.0, -0.0, 1.0, -1.0, 2.0 ** -14, -(2.0 ** -24)]
+    w = rng.integers(1, 300, n).astype(np.float32)
+    coords = np.stack([np.arange(n_blocks), np.zeros(n_blocks), np.zeros(n_blocks)], 1).astype(np.int32)
+    m = rf.MapStruct(synth.intrinsics(64, 48))
+    m.create_config(1 << 12, 1 << 8, 0.008, 0.024, rf.VOXEL_F16)
+    m.import_blocks(coords, s.reshape(n_blocks, 512), w.reshape(n_blocks, 512))
+    c, sd, wt = m.export()
+    order = np.argsort(c[:, 0])
+    got_s, got_w = sd[order].reshape(-1), wt[order].reshape(-1)
+    want_s, want_w = _f16_word_model(s, w)
+    assert np.array_equal(got_s.view(np.int32), want_s.view(np.int32))
+    assert np.array_equal(got_w, want_w)
+    normal = np.abs(s) >= 2.0 ** -14
+    err = np.abs(got_s.astype(np.float64) - s)
+    assert np.all(err[normal] <= 2.0 ** -19 * np.abs(s[normal]))
+    assert err[~normal].max() <= 2.0 ** -25
+    assert np.all(np.signbit(got_s) == np.signbit(s))
+
+
 def test_reset_clears_map(cuda):
     W, H = 160, 120
     K = synth.intrinsics(W, H)

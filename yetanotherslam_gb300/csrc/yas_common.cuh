@@ -146,12 +146,19 @@ struct VoxelIO<YAS_VOXEL_F16> {
     }
     __device__ __forceinline__ static int wt(T v) { return (int)(v >> 24); }
     __device__ __forceinline__ static T make(float s, int w) {
-        const unsigned short hb = __half_as_ushort(__float2half_rn(s));
+        unsigned short hb = __half_as_ushort(__float2half_rn(s));
         int q = 0;
         if (hb & 0x7fffu) {  // h and s share the sign; d = |s| - |h| in FP32 bit units
             const int d = (__float_as_int(s) & 0x7fffffff) -
                           (__float_as_int(__half2float(__ushort_as_half(hb))) & 0x7fffffff);
-            q = max(-128, min(127, (d + 16) >> 5));
+            q = (d + 16) >> 5;  // -128..128 for a normal half
+            if (q > 127 && (hb & 0x7c00u)) {
+                // a tie rounded down: the next half up in magnitude is 2^13
+                // FP32 bit units further, so the same value is q - 256 from it
+                hb = (unsigned short)(hb + 1u);
+                q -= 256;
+            }
+            q = max(-128, min(127, q));  // clamps only below the half's normal range
         }
         return (unsigned)hb | (((unsigned)q & 0xffu) << 16) | ((unsigned)min(w, 255) << 24);
     }
