@@ -69,7 +69,11 @@ enum yas_voxel_format {
     YAS_VOXEL_F32 = 0, /* float sdf + float weight, 8 B/voxel              */
     YAS_VOXEL_F16 = 1, /* fp16 sdf + u8 weight, 4 B/voxel; the spare byte  *
                         * keeps the fp16 rounding residual (1/256 ulp)    */
-    YAS_VOXEL_S24 = 2  /* 24-bit fixed-point sdf (2^-22 step) + u8 weight, 4 B */
+    YAS_VOXEL_S24 = 2, /* 24-bit fixed-point sdf (2^-22 step) + u8 weight, 4 B */
+    YAS_VOXEL_S16 = 3  /* the reference's Voxel {short sdf; uchar wt;}, 4 B and *
+                        * the same byte layout: sdf stored as (short)(s*32767) *
+                        * truncated toward zero, read as q/32767 (PackFloat / *
+                        * UnPackFloat, VoxelStructUtils.h:6-14)                */
 };
 
 typedef struct yas_map_config {

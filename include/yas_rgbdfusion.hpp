@@ -277,7 +277,7 @@ public:
         voxelSize = voxelSize_, truncationDist = truncationDist_;
         sync_pose_to_handle();
     }
-    /* Explicit grid and storage format (F32 / F16 / S24). */
+    /* Explicit grid and storage format (F32 / F16 / S24 / S16). */
     void create(const yas_map_config &cfg) {
         Release();
         check(yas_map_create(&handle_, &cfg, &mK, nullptr));

@@ -23,6 +23,7 @@ _F = C.c_float
 _SIGS = {
     "orc_map_create": ([_F, _F, _F, _F, _I], _P),
     "orc_map_destroy": ([_P], None),
+    "orc_map_set_storage": ([_P, _I], None),
     "orc_map_num_blocks": ([_P], _I),
     "orc_map_allocate": ([_P, _P, _I, _I, _P, _P], None),
     "orc_map_visible": ([_P, _I, _I, _P, _P, _P, _I], _I),
@@ -83,9 +84,13 @@ def _pose(T) -> np.ndarray:
 
 class Map:
     def __init__(self, voxel_size: float, trunc: float, depth_min: float = 0.1, depth_max: float = 3.0,
-                 max_weight: int = 255, kind: str = "f64"):
+                 max_weight: int = 255, kind: str = "f64", int16_sdf: bool = False):
+        """int16_sdf: every written sdf goes through the reference's int16 storage
+        (PackFloat / UnPackFloat, VoxelStructUtils.h:6-14)."""
         self.L = lib(kind)
         self.h = self.L.orc_map_create(voxel_size, trunc, depth_min, depth_max, max_weight)
+        if int16_sdf:
+            self.L.orc_map_set_storage(self.h, 1)
 
     def __del__(self):
         if getattr(self, "h", None):

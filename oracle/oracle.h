@@ -43,6 +43,8 @@ extern "C" {
 typedef struct orc_map orc_map;
 
 orc_map *orc_map_create(float voxel_size, float trunc, float depth_min, float depth_max, int max_weight);
+/* 1: every written sdf goes through the reference's int16 storage. */
+void orc_map_set_storage(orc_map *m, int int16_sdf);
 void orc_map_destroy(orc_map *m);
 int orc_map_num_blocks(const orc_map *m);
 /* Allocation only (CreateBlockLineTracingFunctor). K = {fx, fy, cx, cy}. */

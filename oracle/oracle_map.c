@@ -21,6 +21,7 @@
 struct orc_map {
     float vs, trunc, dmin, dmax;
     int max_w;
+    int q16; /* storage of the reference's int16 sdf (orc_map_set_storage) */
     int n, cap;
     int *coords;
     real *sdf;
@@ -269,6 +270,20 @@ int orc_map_visible(orc_map *m, int cols, int rows, const float *K, const double
     return n;
 }
 
+/* A written sdf as the map keeps it: as computed, or with the reference's
+ * int16 storage (PackFloat / UnPackFloat, VoxelStructUtils.h:6-14): the
+ * FP32 product s * 32767 truncated toward zero, read back as q / 32767. */
+static real stored(const orc_map *m, real s) {
+    if (!m->q16) return s;
+    const float p = (float)s * 32767.0f;
+    int q = (int)p;
+    if (q > 32767) q = 32767;
+    if (q < -32767) q = -32767;
+    return (real)((float)q / 32767.0f);
+}
+
+void orc_map_set_storage(orc_map *m, int int16_sdf) { m->q16 = int16_sdf != 0; }
+
 /* Integration (VoxelMap.cu:738-785): pixel selection and gates in FP32, the
  * running weighted average in `real`. */
 /* sign = +1: DepthFusionFunctor (VoxelMap.cu:719-786); sign = -1: the same
@@ -304,17 +319,17 @@ static void integrate(orc_map *m, const float *depth, int w, int h, const float 
                     const int wt = m->wt[k];
                     if (sign > 0) {
                         if (wt == 0) {
-                            m->sdf[k] = sdf;
+                            m->sdf[k] = stored(m, sdf);
                             m->wt[k] = 1;
                         } else {
-                            m->sdf[k] = (m->sdf[k] * (real)wt + sdf) / (real)(wt + 1);
+                            m->sdf[k] = stored(m, (m->sdf[k] * (real)wt + sdf) / (real)(wt + 1));
                             m->wt[k] = wt + 1 < m->max_w ? wt + 1 : m->max_w;
                         }
                     } else if (wt == 1) {
                         m->sdf[k] = 0;
                         m->wt[k] = 0;
                     } else if (wt > 1) {
-                        m->sdf[k] = (m->sdf[k] * (real)wt - sdf) / (real)(wt - 1);
+                        m->sdf[k] = stored(m, (m->sdf[k] * (real)wt - sdf) / (real)(wt - 1));
                         m->wt[k] = wt - 1;
                     }
                 }
@@ -465,7 +480,7 @@ int orc_map_fuse_map(orc_map *dst, orc_map *src, const double *Tdst, const doubl
             const size_t k = (size_t)b * 512 + li;
             const int dw = dst->wt[k];
             const real ds = dw ? dst->sdf[k] : 0;
-            dst->sdf[k] = (ds * (real)dw + sv * (real)w0) / (real)(dw + w0);
+            dst->sdf[k] = stored(dst, (ds * (real)dw + sv * (real)w0) / (real)(dw + w0));
             dst->wt[k] = dw + w0 < dst->max_w ? dw + w0 : dst->max_w;
         }
     }

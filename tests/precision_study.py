@@ -130,11 +130,13 @@ def run(frames: int = 300, W: int = 640, H: int = 480, voxel: float = 0.005, see
     # mapping: maps fused with the oracle's poses and the same depth, so the
     # TSDF and mesh differences are those of the storage and arithmetic alone
     maps = {}
-    for fname, fmt in (("f32", rf.VOXEL_F32), ("f16", rf.VOXEL_F16), ("s24", rf.VOXEL_S24)):
+    for fname, fmt in (("f32", rf.VOXEL_F32), ("f16", rf.VOXEL_F16), ("s24", rf.VOXEL_S24), ("s16", rf.VOXEL_S16)):
         m = rf.MapStruct(K)
         m.create_config(slots, blocks, voxel, trunc, fmt)
         maps[fname] = m
     omap = oracle.Map(voxel, trunc)
+    # the reference's own int16 storage, restated in the oracle (parity of s16)
+    omap16 = oracle.Map(voxel, trunc, int16_sdf=True)
     mesher = rf.MeshEngine(8_000_000)
     # open loop: standalone trackers given exactly the oracle session's inputs
     # of each frame (previous frame as reference, the oracle's raycast model)
@@ -212,12 +214,14 @@ def run(frames: int = 300, W: int = 640, H: int = 480, voxel: float = 0.005, see
         for m in maps.values():
             m.Fuse(dm, To)
         omap.fuse(dm, K, To)
+        omap16.fuse(dm, K, To)
         if (i + 1) % mc_every == 0 or i + 1 == frames:
             row = {"frame": i + 1, "mapping": {}, "tracked": {}}
             o_exp, o_mesh = omap.export(), omap.mesh(8_000_000)
             for fname, m in maps.items():
                 row["mapping"][fname] = {"tsdf": tsdf_error(m.export(), o_exp),
                                          "mesh": mesh_error(mesher.Meshify(m), o_mesh)}
+            row["s16_vs_int16_oracle"] = tsdf_error(maps["s16"].export(), omap16.export())
             so_exp = orc.map_export()
             for name, s in sessions.items():
                 row["tracked"][name] = {"tsdf": tsdf_error(s.map().export(), so_exp)}
@@ -270,6 +274,9 @@ def summary(report: dict) -> str:
         vm = max(c["mapping"][f]["mesh"]["max"] for c in ck)
         vp = max(c["mapping"][f]["mesh"]["p99"] for c in ck)
         lines.append(f"| {f} | {tm:.2e} | {tp:.2e} | {eq:.4f} | {sc:.5f} | {vm:.2e} | {vp:.2e} |")
+    p16 = [c["s16_vs_int16_oracle"] for c in ck]
+    lines += ["", f"s16 against the oracle keeping the same int16 storage: TSDF max {max(x['max'] for x in p16):.2e}, "
+              f"p99 {max(x['p99'] for x in p16):.2e}, weights equal {min(x['weight_equal_frac'] for x in p16):.4f}"]
     last = ck[-1]["mapping"]["f32"]
     lines += ["", f"final map: {last['tsdf']['blocks_oracle']} blocks, {last['mesh']['triangles_oracle']} "
               f"triangles (oracle); {report['seconds']:.0f} s"]

@@ -40,7 +40,7 @@ def _fused_map(fmt, W=640, H=480, n=5, vs=0.008):
     return K, poses, m, o
 
 
-@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16])
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16, rf.VOXEL_S16])
 def test_raycast_matches_oracle(cuda, fmt):
     W, H = 640, 480
     K, poses, m, o = _fused_map(fmt)
@@ -94,7 +94,7 @@ def _sorted_soup(pts, nrm, cases, cube):
     return pts[order], nrm[order], cases[order], cube[order]
 
 
-@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_S24])
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_S24, rf.VOXEL_S16])
 def test_marching_cubes_matches_oracle(cuda, fmt):
     K, poses, m, o = _fused_map(fmt, n=3)
     me = rf.MeshEngine(4_000_000)

@@ -22,7 +22,7 @@ STATUS = {
     9: "YAS_ERR_STATE", 10: "YAS_ERR_COORD_RANGE", 11: "YAS_ERR_CAPACITY", 12: "YAS_ERR_TIMEOUT",
     13: "YAS_ERR_IO",
 }
-VOXEL_F32, VOXEL_F16, VOXEL_S24 = 0, 1, 2
+VOXEL_F32, VOXEL_F16, VOXEL_S24, VOXEL_S16 = 0, 1, 2, 3
 TRACK_RGB, TRACK_ICP, TRACK_RGBD = 1, 2, 3
 
 

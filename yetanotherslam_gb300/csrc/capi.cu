@@ -178,7 +178,7 @@ YAS_API int yas_map_create(yas_map **out, const yas_map_config *cfg, const yas_i
     if (!out || !cfg || !K) return YAS_ERR_BAD_ARG;
     *out = nullptr;
     if (!is_pow2(cfg->hash_slots) || cfg->max_blocks <= 0 || !(cfg->voxel_size > 0.0f) ||
-        !(cfg->trunc_dist > 0.0f) || cfg->voxel_format < 0 || cfg->voxel_format > 2 || cfg->max_weight < 1 ||
+        !(cfg->trunc_dist > 0.0f) || cfg->voxel_format < 0 || cfg->voxel_format > 3 || cfg->max_weight < 1 ||
         cfg->max_weight > 65535 || (cfg->voxel_format != YAS_VOXEL_F32 && cfg->max_weight > 255))
         return YAS_ERR_BAD_ARG;
     yas_map *m = new yas_map();

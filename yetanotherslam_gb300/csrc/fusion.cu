@@ -171,6 +171,9 @@ void launch_fuse_alloc(const MapDev &dst, const MapDev &src, int fmt, const Rigi
         case YAS_VOXEL_F16:
             fuse_alloc_kernel<YAS_VOXEL_F16><<<grid, 256, 0, s>>>(dst, src, T_src_dst, nsrc);
             break;
+        case YAS_VOXEL_S16:
+            fuse_alloc_kernel<YAS_VOXEL_S16><<<grid, 256, 0, s>>>(dst, src, T_src_dst, nsrc);
+            break;
         default:
             fuse_alloc_kernel<YAS_VOXEL_S24><<<grid, 256, 0, s>>>(dst, src, T_src_dst, nsrc);
             break;
@@ -185,6 +188,9 @@ void launch_fuse_blend(const MapDev &dst, const MapDev &src, int fmt, const Rigi
             break;
         case YAS_VOXEL_F16:
             fuse_blend_kernel<YAS_VOXEL_F16><<<grid, 256, 0, s>>>(dst, src, T_dst_src);
+            break;
+        case YAS_VOXEL_S16:
+            fuse_blend_kernel<YAS_VOXEL_S16><<<grid, 256, 0, s>>>(dst, src, T_dst_src);
             break;
         default:
             fuse_blend_kernel<YAS_VOXEL_S24><<<grid, 256, 0, s>>>(dst, src, T_dst_src);

@@ -308,6 +308,9 @@ static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, 
         case YAS_VOXEL_F16:
             integrate_kernel<YAS_VOXEL_F16, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
             break;
+        case YAS_VOXEL_S16:
+            integrate_kernel<YAS_VOXEL_S16, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            break;
         default:
             integrate_kernel<YAS_VOXEL_S24, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
             break;
@@ -375,6 +378,8 @@ void launch_map_export(const MapDev &m, int fmt, int *coords, float *sdf, float 
         export_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, coords, sdf, wt, first, count);
     else if (fmt == YAS_VOXEL_F16)
         export_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, coords, sdf, wt, first, count);
+    else if (fmt == YAS_VOXEL_S16)
+        export_kernel<YAS_VOXEL_S16><<<grid, 128, 0, s>>>(m, coords, sdf, wt, first, count);
     else
         export_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, coords, sdf, wt, first, count);
 }
@@ -432,6 +437,8 @@ void launch_map_import(const MapDev &m, int fmt, const int *coords, const float 
         import_kernel<YAS_VOXEL_F32><<<256, 256, 0, s>>>(m, coords, sdf, wt, count);
     else if (fmt == YAS_VOXEL_F16)
         import_kernel<YAS_VOXEL_F16><<<256, 256, 0, s>>>(m, coords, sdf, wt, count);
+    else if (fmt == YAS_VOXEL_S16)
+        import_kernel<YAS_VOXEL_S16><<<256, 256, 0, s>>>(m, coords, sdf, wt, count);
     else
         import_kernel<YAS_VOXEL_S24><<<256, 256, 0, s>>>(m, coords, sdf, wt, count);
 }

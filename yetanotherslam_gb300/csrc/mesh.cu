@@ -403,6 +403,9 @@ int launch_meshify(const MapDev &m, int fmt, MeshBuffers &mb, unsigned n_blocks,
         case YAS_VOXEL_F16:
             mc_count_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
             break;
+        case YAS_VOXEL_S16:
+            mc_count_kernel<YAS_VOXEL_S16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
+            break;
         default:
             mc_count_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);
             break;
@@ -415,6 +418,10 @@ int launch_meshify(const MapDev &m, int fmt, MeshBuffers &mb, unsigned n_blocks,
             break;
         case YAS_VOXEL_F16:
             mc_emit_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+                                                               mb.points, mb.normals, mb.cases, mb.cube_xyz);
+            break;
+        case YAS_VOXEL_S16:
+            mc_emit_kernel<YAS_VOXEL_S16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
                                                                mb.points, mb.normals, mb.cases, mb.cube_xyz);
             break;
         default:

@@ -437,10 +437,10 @@ __global__ void __launch_bounds__(128) march_persistent_kernel(MapDev m, Cam cam
 }
 
 static int march_resident_ctas(int fmt) {
-    static int cache[3][64];
+    static int cache[4][64];
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || fmt < 0 || fmt > 2) return 152;
+    if (dev < 0 || dev >= 64 || fmt < 0 || fmt > 3) return 152;
     int &c = cache[fmt][dev];
     if (c == 0) {
         int sms = 0, nb = 0;
@@ -449,6 +449,8 @@ static int march_resident_ctas(int fmt) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_F32>, 128, 0);
         else if (fmt == YAS_VOXEL_F16)
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_F16>, 128, 0);
+        else if (fmt == YAS_VOXEL_S16)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_S16>, 128, 0);
         else
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_persistent_kernel<YAS_VOXEL_S24>, 128, 0);
         cudaGetLastError();
@@ -471,6 +473,10 @@ static void launch_march_persistent(const MapDev &m, int fmt, const Cam &cam, co
             march_persistent_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
                                                                         vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
             break;
+        case YAS_VOXEL_S16:
+            march_persistent_kernel<YAS_VOXEL_S16><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                        vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
+            break;
         default:
             march_persistent_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
                                                                         vmap_pitch_elems, skip, rb.queue, total, rb.fnear, rb.fw);
@@ -490,6 +496,10 @@ static void launch_march_tile(const MapDev &m, int fmt, const Cam &cam, const Po
             break;
         case YAS_VOXEL_F16:
             march_kernel<YAS_VOXEL_F16, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
+                                                                         vmap_pitch_elems, skip, rb.fnear, rb.fw);
+            break;
+        case YAS_VOXEL_S16:
+            march_kernel<YAS_VOXEL_S16, WX, WY><<<grid, threads, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, vmap,
                                                                          vmap_pitch_elems, skip, rb.fnear, rb.fw);
             break;
         default:

@@ -179,6 +179,25 @@ struct VoxelIO<YAS_VOXEL_S24> {
     }
 };
 
+// The reference's voxel (VoxelMap.h:26-30: short sdf, uchar wt, padded to 4
+// bytes; the word's bytes are the struct's): bits 0..15 the int16 sdf, bits
+// 16..23 the weight.  PackFloat / UnPackFloat (VoxelStructUtils.h:6-14): the
+// sdf is stored as (short)(s * 32767), truncated toward zero, and read back
+// with an IEEE division by 32767.
+template <>
+struct VoxelIO<YAS_VOXEL_S16> {
+    typedef unsigned T;
+    static constexpr int kBytes = 4;
+    __device__ __forceinline__ static float sdf(T v) {
+        return __fdiv_rn((float)(short)(v & 0xffffu), 32767.0f);
+    }
+    __device__ __forceinline__ static int wt(T v) { return (int)((v >> 16) & 0xffu); }
+    __device__ __forceinline__ static T make(float s, int w) {
+        const int q = max(-32767, min(32767, __float2int_rz(__fmul_rn(s, 32767.0f))));
+        return ((unsigned)q & 0xffffu) | ((unsigned)min(w, 255) << 16);
+    }
+};
+
 // ------------------------------------------------------------------ map view
 struct MapDev {
     HashSlot *slots;

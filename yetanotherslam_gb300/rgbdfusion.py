@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib as L
 
-VOXEL_F32, VOXEL_F16, VOXEL_S24 = L.VOXEL_F32, L.VOXEL_F16, L.VOXEL_S24
+VOXEL_F32, VOXEL_F16, VOXEL_S24, VOXEL_S16 = L.VOXEL_F32, L.VOXEL_F16, L.VOXEL_S24, L.VOXEL_S16
 TRACK_RGB, TRACK_ICP, TRACK_RGBD = L.TRACK_RGB, L.TRACK_ICP, L.TRACK_RGBD
 
 
