@@ -642,7 +642,7 @@ __device__ __forceinline__ void fused_pixel_b(const LevelCam &c, float th, const
 // the 32 warp sums of each value), of which warp 0 publishes words
 // first..first+count-1 as tagged words.  Each value's sum does not depend on
 // the others, so publishing a row in two ranges gives the same words.  The
-// caller separates two calls with a barrier (wsum is reused); v is consumed.
+// caller separates two calls with a barrier (wsum is reused).
 __device__ __forceinline__ void fused_publish_row(float v[32], unsigned long long *row, unsigned tag,
                                                   unsigned first = 0, unsigned count = 32) {
     __shared__ float wsum[kFusedWarps][33];
@@ -848,8 +848,6 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     }
                 }
                 fused_publish_row(acc, rA + cta * 32, tag, 29, 3);
-#pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] = 0.0f;  // the reduction left partial sums in acc
             }
             if (do_icp) {
                 if constexpr (PIX > 0) {
