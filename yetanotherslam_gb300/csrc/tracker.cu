@@ -536,15 +536,16 @@ __device__ __forceinline__ bool poll_continue(GNState *st, unsigned spin, unsign
     return true;
 }
 
-// Pass A for one pixel, photometric half: the residual (kept for pass B) and
-// its moments, accumulated as gn_pass_a does.
-__device__ __forceinline__ void fused_pixel_rgb(const FusedLevel &lv, const float *sT, const float *sRK, int k,
-                                                float acc[32], float4 &res, float3 &p) {
+// Pass A for one pixel: the photometric residual (kept in registers for pass
+// B) and the ICP products, accumulated as gn_pass_a does.
+__device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float *sT, const float *sRK, int k,
+                                              bool do_rgb, bool do_icp, float angle_th, float dist_th,
+                                              float acc[32], float4 &res, float3 &p) {
     const LevelCam &c = lv.c;
     const int y = k / c.w, x = k - y * c.w;
     res = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
     p = make_float3(0.0f, 0.0f, 1.0f);
-    {
+    if (do_rgb) {
         const float zinv = __ldg(lv.ref_invd + k);
         if (zinv > 0.0f) {
             const float z = 1.0f / zinv;
@@ -565,14 +566,7 @@ __device__ __forceinline__ void fused_pixel_rgb(const FusedLevel &lv, const floa
             }
         }
     }
-}
-
-// Pass A for one pixel, ICP half: the point-to-plane products, accumulated as
-// gn_pass_a does.
-__device__ __forceinline__ void fused_pixel_icp(const FusedLevel &lv, const float *sT, int k, float angle_th,
-                                                float dist_th, float acc[32]) {
-    const LevelCam &c = lv.c;
-    {
+    if (do_icp) {
         const float4 vm = __ldg(lv.ref_vmap + k);
         if (vm.w >= 0.0f) {
             const float3 vl = make_float3(sT[0] * vm.x + sT[1] * vm.y + sT[2] * vm.z + sT[3],
@@ -639,12 +633,8 @@ __device__ __forceinline__ void fused_pixel_b(const LevelCam &c, float th, const
 
 
 // The CTA's row of 32 sums (warp transpose sums, then a pairwise tree over
-// the 32 warp sums of each value), of which warp 0 publishes words
-// first..first+count-1 as tagged words.  Each value's sum does not depend on
-// the others, so publishing a row in two ranges gives the same words.  The
-// caller separates two calls with a barrier (wsum is reused).
-__device__ __forceinline__ void fused_publish_row(float v[32], unsigned long long *row, unsigned tag,
-                                                  unsigned first = 0, unsigned count = 32) {
+// the 32 warp sums of each value), published by warp 0 as tagged words.
+__device__ __forceinline__ void fused_publish_row(float v[32], unsigned long long *row, unsigned tag) {
     __shared__ float wsum[kFusedWarps][33];
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const float r = warp_transpose_reduce(v);
@@ -658,7 +648,7 @@ __device__ __forceinline__ void fused_publish_row(float v[32], unsigned long lon
         for (int s = kFusedWarps / 2; s >= 1; s >>= 1)
 #pragma unroll
             for (int i = 0; i < s; ++i) x[i] += x[i + s];
-        if (lane - first < count) st_relaxed_u64(row + lane, tagged(x[0], tag));
+        st_relaxed_u64(row + lane, tagged(x[0], tag));
     }
 }
 
@@ -819,55 +809,28 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             for (int i = 0; i < 32; ++i) acc[i] = 0.0f;
             float4 res[PIX > 0 ? PIX : 1];
             float3 pp[PIX > 0 ? PIX : 1];
+            if constexpr (PIX > 0) {
 #pragma unroll
-            for (int q = 0; q < (PIX > 0 ? PIX : 1); ++q) {
-                res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-                pp[q] = make_float3(0.0f, 0.0f, 1.0f);
-            }
-            // pass A, photometric half first: its moments (words 29..31) are
-            // published before the ICP half runs, so the moment fold's wait
-            // overlaps the ICP products (words 0..28)
-            if (do_rgb) {
-                if constexpr (PIX > 0) {
-#pragma unroll
-                    for (int q = 0; q < PIX; ++q) {
-                        const int off = q * kFusedThreads + t;
-                        const int k = base + off;
-                        if (q < lv.pix && off < lv.chunk && k < n)
-                            fused_pixel_rgb(lv, g_solve.Tf, sRK, k, acc, res[q], pp[q]);
-                    }
-                } else {
-#pragma unroll 2
-                    for (int off = t; off < lv.chunk; off += kFusedThreads) {
-                        const int k = base + off;
-                        if (k >= n) break;
-                        float4 r4;
-                        float3 p3;
-                        fused_pixel_rgb(lv, g_solve.Tf, sRK, k, acc, r4, p3);
-                        res4[k] = r4;
-                    }
+                for (int q = 0; q < PIX; ++q) {
+                    res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                    pp[q] = make_float3(0.0f, 0.0f, 1.0f);
+                    const int off = q * kFusedThreads + t;
+                    const int k = base + off;
+                    if (q < lv.pix && off < lv.chunk && k < n)
+                        fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, res[q], pp[q]);
                 }
-                fused_publish_row(acc, rA + cta * 32, tag, 29, 3);
-            }
-            if (do_icp) {
-                if constexpr (PIX > 0) {
-#pragma unroll
-                    for (int q = 0; q < PIX; ++q) {
-                        const int off = q * kFusedThreads + t;
-                        const int k = base + off;
-                        if (q < lv.pix && off < lv.chunk && k < n) fused_pixel_icp(lv, g_solve.Tf, k, angle_th, dist_th, acc);
-                    }
-                } else {
+            } else {
 #pragma unroll 2
-                    for (int off = t; off < lv.chunk; off += kFusedThreads) {
-                        const int k = base + off;
-                        if (k >= n) break;
-                        fused_pixel_icp(lv, g_solve.Tf, k, angle_th, dist_th, acc);
-                    }
+                for (int off = t; off < lv.chunk; off += kFusedThreads) {
+                    const int k = base + off;
+                    if (k >= n) break;
+                    float4 r4;
+                    float3 p3;
+                    fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, r4, p3);
+                    if (do_rgb) res4[k] = r4;
                 }
-                __syncthreads();  // the photometric half's publish has read wsum
-                fused_publish_row(acc, rA + cta * 32, tag, 0, 29);
             }
+            fused_publish_row(acc, rA + cta * 32, tag);
             if (do_rgb) {
                 if (!fold_moments(rA, nrows, tag, st, plain)) return;
                 if (t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
