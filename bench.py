@@ -417,7 +417,7 @@ def run_served(seed: int = 100, gn_per_session: bool | None = None):
 
 BATCHED = {"submaps": 16, "resolutions": [[320, 240], [480, 360], [640, 480]], "voxel_m": [0.005, 0.008],
            "frames": [5, 60], "hash_slots": 1 << 20, "max_blocks": 1 << 17, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)",
-           "calibration_frames": 4}
+           "calibration_frames": 6}
 
 
 def run_batched(seed: int = 7, only_pass: bool = False):

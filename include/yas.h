@@ -500,9 +500,11 @@ YAS_API int yas_batch_kernels_per_step(yas_batch *b, int *out);
  * knob (GN share, march CTA shape, integration grid) is tried in turn over a
  * few candidate values (GN share, GN launches per session or per step, march
  * CTA shape, integration grid), the others held, each candidate timed by the median
- * device time of its steps.  The fastest value is kept, applied to the batch
- * and written to *out (may be NULL).  The batch's own sessions are not
- * touched. */
+ * device time of its tracked steps over three passes.  A value replaces the
+ * current one only if it is more than 3 % faster, and the final choice must
+ * beat the starting tuning by that margin again when both are re-measured.
+ * It is applied to the batch and written to *out (may be NULL).  The batch's
+ * own sessions are not touched. */
 YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const uint16_t *const *depth, int frames,
                                int on_device, yas_batch_tuning *out);
 

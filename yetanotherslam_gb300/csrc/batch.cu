@@ -513,28 +513,36 @@ YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const ui
     std::vector<const uint8_t *> fr(n);
     std::vector<const uint16_t *> fd(n);
     std::vector<float> ms;
-    // median device time of one pass over the calibration frames (tracked steps)
+    // median device time of the tracked steps of kPasses passes over the
+    // calibration frames (the sessions restarted before each pass)
+    constexpr int kPasses = 3;
     auto measure = [&](const yas_batch_tuning &t, float *median) -> int {
         YAS_TRY(yas_batch_set_tuning(cb, &t));
-        for (yas_session *c : clones) YAS_TRY(session_restart(c));
         ms.clear();
-        for (int f = 0; f < frames; ++f) {
-            for (size_t i = 0; i < n; ++i) {
-                const yas_session_config &c = session_config(clones[i]);
-                const size_t px = (size_t)c.width * c.height;
-                fr[i] = rgb[i] + (size_t)f * px * 3;
-                fd[i] = depth[i] + (size_t)f * px;
+        for (int pass = 0; pass < kPasses; ++pass) {
+            for (yas_session *c : clones) YAS_TRY(session_restart(c));
+            for (int f = 0; f < frames; ++f) {
+                for (size_t i = 0; i < n; ++i) {
+                    const yas_session_config &c = session_config(clones[i]);
+                    const size_t px = (size_t)c.width * c.height;
+                    fr[i] = rgb[i] + (size_t)f * px * 3;
+                    fd[i] = depth[i] + (size_t)f * px;
+                }
+                YAS_TRY(yas_batch_step(cb, fr.data(), fd.data(), nullptr, on_device));
+                float t_ms = 0.0f;
+                YAS_TRY(yas_batch_wait(cb, nullptr, nullptr, &t_ms));
+                if (f > 0) ms.push_back(t_ms);
             }
-            YAS_TRY(yas_batch_step(cb, fr.data(), fd.data(), nullptr, on_device));
-            float t_ms = 0.0f;
-            YAS_TRY(yas_batch_wait(cb, nullptr, nullptr, &t_ms));
-            if (f > 0) ms.push_back(t_ms);
         }
         std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
         *median = ms[ms.size() / 2];
         return YAS_OK;
     };
-    yas_batch_tuning best = b->tuning;
+    // a candidate replaces the incumbent only if it is faster by more than
+    // this fraction, so timing noise does not move the tuning
+    constexpr float kMargin = 0.03f;
+    const yas_batch_tuning start = b->tuning;
+    yas_batch_tuning best = start;
     float best_ms = 0.0f;
     if (st == YAS_OK) st = measure(best, &best_ms);
     // coordinate descent, one pass: GN share, GN launches, march CTA shape, integration grid
@@ -554,11 +562,19 @@ YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const ui
             *field = value;
             float m = 0.0f;
             st = measure(t, &m);
-            if (st == YAS_OK && m < best_ms) {
+            if (st == YAS_OK && m < best_ms * (1.0f - kMargin)) {
                 best_ms = m;
                 best = t;
             }
         }
+    }
+    // confirmation: the winner against the starting tuning, measured again
+    // side by side; the starting tuning stays unless the winner still wins
+    if (st == YAS_OK && memcmp(&best, &start, sizeof(best)) != 0) {
+        float m_start = 0.0f, m_best = 0.0f;
+        st = measure(start, &m_start);
+        if (st == YAS_OK) st = measure(best, &m_best);
+        if (st == YAS_OK && !(m_best < m_start * (1.0f - kMargin))) best = start;
     }
     if (cb) yas_batch_destroy(cb);
     for (yas_session *c : clones)
