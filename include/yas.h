@@ -260,6 +260,14 @@ YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused);
  * either way.  Takes effect at the next GetTransform, captured graphs
  * included. */
 YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated);
+/* Checks the fused GN schedule's bounded waits (no counterpart in the
+ * reference).  Runs the schedule on the tracker's current images as a launch
+ * whose descriptor names two CTAs but starts one, so the waits for the missing
+ * CTA's partial sums run out: after about 1 s the schedule records a timeout
+ * and ends.  *out_status receives what the schedule reports (YAS_ERR_TIMEOUT
+ * when the limit works).  The tracker stays usable; its next GetTransform
+ * starts from a reset state.  Takes about one second. */
+YAS_API int yas_tracker_check_wait_limit(yas_tracker *tr, int *out_status);
 /* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);

@@ -11,7 +11,11 @@ RGBDFusion/include/TrackingUtils.h.  Bars:
     distance between the oracle's own FP64 and FP32 builds on the same inputs
     (zero unless FP32 arithmetic flips GetTransform's keep-the-better-estimate
     decision on a near-tie, RGBDTracking.cu:184-199; the reference computes in
-    FP32 too).
+    FP32 too);
+  * bounded waits: the fused schedule launched with one of its two CTAs
+    missing reports YAS_ERR_TIMEOUT after its 1 s limit (a wait that nothing
+    ends, made on purpose, without a fault), and the tracker then tracks as
+    before, bit for bit.
 """
 from __future__ import annotations
 
@@ -177,3 +181,20 @@ def test_tracking_from_no_data_returns_identity(cuda):
     tr.SetTrackingDepth(z)
     T = tr.GetTransform(np.eye(4), True)
     assert np.allclose(T, np.eye(4))
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_bounded_wait_reports_timeout_and_tracker_recovers(cuda, mode):
+    import time
+
+    tr, _, _ = _setup(mode, W=160, H=120, levels=2, iters=(3, 2))
+    tr.set_schedule(True)
+    before = tr.GetTransform(np.eye(4), False)
+    t0 = time.perf_counter()
+    status = tr.check_wait_limit()
+    dt = time.perf_counter() - t0
+    assert status == 12, status  # YAS_ERR_TIMEOUT
+    assert 0.9 <= dt < 10.0, dt
+    assert not tr.IsTrackingGood()
+    after = tr.GetTransform(np.eye(4), False)
+    assert tr.IsTrackingGood() and np.array_equal(before, after)

@@ -121,6 +121,7 @@ _SIGS = {
     "yas_map_reset_visible": [_P],
     "yas_copy_to_host": [_P, _I, _P, _I, _I, _I],
     "yas_tracker_set_reduction": [_P, _I],
+    "yas_tracker_check_wait_limit": [_P, _PI],
     "yas_pyr_down_depth": [_P, _I, _I, _I, _P, _I, _I, _I, _P],
     "yas_depth_to_inv_depth": [_P, _I, _I, _I, _P, _I, _P],
     "yas_compute_vertex_map": [_P, _I, _I, _I, _P, _I, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _P],

@@ -1229,6 +1229,42 @@ YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated) {
     return YAS_OK;
 }
 
+YAS_API int yas_tracker_check_wait_limit(yas_tracker *tr, int *out_status) {
+    if (!tr || !out_status) return YAS_ERR_BAD_ARG;
+    if (gn_batch_capacity() < 2) return YAS_ERR_STATE;
+    GNBatchItem *d_item = nullptr;
+    unsigned short *d_map = nullptr;
+    if (cudaMalloc(&d_item, sizeof(GNBatchItem)) != cudaSuccess ||
+        cudaMalloc(&d_map, 2 * sizeof(unsigned short)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_item);
+        return YAS_ERR_OOM;
+    }
+    // every index in range: the descriptor's chunks are those of two CTAs and
+    // CTA 0 touches only its own; only the missing CTA's rows never arrive
+    GNBatchItem it;
+    gn_batch_item_ctas(tr, 0, 2, &it);
+    cudaError_t e = cudaMemcpyAsync(d_item, &it, sizeof(it), cudaMemcpyHostToDevice, tr->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_map, 0, 2 * sizeof(unsigned short), tr->stream);
+    if (e == cudaSuccess) {
+        launch_gn_init(tr, pose_identity(), tr->stream);
+        e = launch_gn_batch(d_item, d_map, 1, tr->stream, gn_batch_pix(&it, 1));
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(tr->state_host, tr->state, sizeof(GNState), cudaMemcpyDeviceToHost, tr->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(tr->stream);
+    cudaFree(d_item);
+    cudaFree(d_map);
+    if (e != cudaSuccess) {
+        record_cuda_error(e, "wait limit check", __FILE__, __LINE__);
+        return YAS_ERR_CUDA;
+    }
+    const int failed = tr->state_host->failed;
+    *out_status = failed == kFailTimeout ? YAS_ERR_TIMEOUT : (failed ? YAS_ERR_NUMERIC : YAS_OK);
+    tr->good = false;
+    return YAS_OK;
+}
+
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out) {
     if (!tr || !out) return YAS_ERR_BAD_ARG;
     *out = tr->good ? 1 : 0;

@@ -363,6 +363,14 @@ class RGBDTracking:
         """Compensated FP32 sums with FP64 totals (True) or plain FP32 sums (False)."""
         L.call("yas_tracker_set_reduction", self.handle, int(compensated))
 
+    def check_wait_limit(self) -> int:
+        """Runs the fused schedule with one of two CTAs missing, so its bounded
+        waits run out (about 1 s); returns the status it reports
+        (YAS_ERR_TIMEOUT, 12, when the limit works)."""
+        out = C.c_int()
+        L.call("yas_tracker_check_wait_limit", self.handle, C.byref(out))
+        return out.value
+
     def IsTrackingGood(self) -> bool:
         out = C.c_int()
         L.call("yas_tracker_is_good", self.handle, C.byref(out))
