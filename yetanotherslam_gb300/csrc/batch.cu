@@ -361,7 +361,7 @@ extern "C" {
 YAS_API int yas_batch_tuning_default(yas_batch_tuning *t) {
     if (!t) return YAS_ERR_BAD_ARG;
     t->march_warps_x = 2;
-    t->integrate_ctas = 152 * 8;
+    t->integrate_ctas = kSMs * 8;
     t->gn_pixels_per_cta = 0;
     t->gn_per_session = 1;
     return YAS_OK;
@@ -548,7 +548,7 @@ YAS_API int yas_batch_autotune(yas_batch *b, const uint8_t *const *rgb, const ui
     // coordinate descent, one pass: GN share, GN launches, march CTA shape, integration grid
     const int gn_c[4] = {0, 16384, 32768, 65536};
     const int mw_c[4] = {0, 1, 2, 4};
-    const int ig_c[4] = {152 * 4, 152 * 8, 152 * 16, 152 * 8};
+    const int ig_c[4] = {kSMs * 4, kSMs * 8, kSMs * 16, kSMs * 8};
     const int ps_c[4] = {0, 1, 1, 1};
     for (int knob = 0; knob < 4 && st == YAS_OK; ++knob) {
         for (int v = 0; v < 4 && st == YAS_OK; ++v) {

@@ -197,7 +197,7 @@ YAS_API int yas_canvas_draw_triangles(yas_canvas *c, const float *points, const 
         p = tmp;
         n = tmp + (size_t)n_tris * 9;
     }
-    const int grid = (int)std::min<unsigned>((n_tris + 127) / 128, 152u * 16u);
+    const int grid = (int)std::min<unsigned>((n_tris + 127) / 128, (unsigned)kSMs * 16u);
     canvas_draw_kernel<<<grid, 128, 0, c->stream>>>(p, n, n_tris, affine_of(*Tmw), affine_of(*Tcw), c->cam, c->keys,
                                                     c->w, c->h);
     cudaError_t e = cudaGetLastError();

@@ -163,7 +163,7 @@ void launch_rehash(const MapDev &m, unsigned n, cudaStream_t s) {
 
 void launch_fuse_alloc(const MapDev &dst, const MapDev &src, int fmt, const Rigid32 &T_src_dst, unsigned nsrc,
                        cudaStream_t s) {
-    const int grid = 152 * 8;
+    const int grid = kSMs * 8;
     switch (fmt) {
         case YAS_VOXEL_F32:
             fuse_alloc_kernel<YAS_VOXEL_F32><<<grid, 256, 0, s>>>(dst, src, T_src_dst, nsrc);
@@ -181,7 +181,7 @@ void launch_fuse_alloc(const MapDev &dst, const MapDev &src, int fmt, const Rigi
 }
 
 void launch_fuse_blend(const MapDev &dst, const MapDev &src, int fmt, const Rigid32 &T_dst_src, cudaStream_t s) {
-    const int grid = 152 * 8;
+    const int grid = kSMs * 8;
     switch (fmt) {
         case YAS_VOXEL_F32:
             fuse_blend_kernel<YAS_VOXEL_F32><<<grid, 256, 0, s>>>(dst, src, T_dst_src);

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) visible_kernel(MapDev m, Cam cam, const P
 
 void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const int *skip,
                     cudaStream_t s) {
-    visible_kernel<<<152 * 4, 256, 0, s>>>(m, cam, P, skip);
+    visible_kernel<<<kSMs * 4, 256, 0, s>>>(m, cam, P, skip);
 }
 
 // ---------------------------------------------------------------- integration
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
 template <int SIGN>
 static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
                                   const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0) {
-    const int grid = grid_ctas > 0 ? grid_ctas : 152 * 8;
+    const int grid = grid_ctas > 0 ? grid_ctas : kSMs * 8;
     switch (fmt) {
         case YAS_VOXEL_F32:
             integrate_kernel<YAS_VOXEL_F32, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
@@ -344,7 +344,7 @@ __global__ void reset_slots_kernel(MapDev m) {
 }
 
 void launch_map_reset(const MapDev &m, cudaStream_t s) {
-    reset_slots_kernel<<<152 * 4, 256, 0, s>>>(m);
+    reset_slots_kernel<<<kSMs * 4, 256, 0, s>>>(m);
 }
 
 // ---------------------------------------------------------------- export/import

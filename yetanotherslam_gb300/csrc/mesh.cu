@@ -395,7 +395,7 @@ int launch_meshify(const MapDev &m, int fmt, MeshBuffers &mb, unsigned n_blocks,
     YAS_TRY(mesher_ensure_blocks(mb, n_blocks));
     cudaMemsetAsync(mb.counters, 0, sizeof(unsigned), s);
     if (n_blocks == 0) return YAS_OK;
-    const unsigned grid = n_blocks < 152u * 16u ? n_blocks : 152u * 16u;
+    const unsigned grid = n_blocks < (unsigned)kSMs * 16u ? n_blocks : (unsigned)kSMs * 16u;
     switch (fmt) {
         case YAS_VOXEL_F32:
             mc_count_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_tris);

@@ -123,7 +123,7 @@ void launch_zrange(const MapDev &m, const Cam &cam, const PosePair *P, RaycastBu
     const int n = rb.zw * rb.zh, nf = rb.fw * rb.fh;
     zrange_reset_kernel<<<(std::max(n, nf) + 255) / 256, 256, 0, s>>>(rb.znear, rb.zfar, n, &m.hdr->n_render,
                                                                       rb.queue, rb.fnear, nf);
-    zrange_fill_kernel<<<152 * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip, rb.fnear, rb.fw,
+    zrange_fill_kernel<<<kSMs * 2, 128, 0, s>>>(m, cam, P, rb.znear, rb.zfar, rb.zw, rb.zh, skip, rb.fnear, rb.fw,
                                                rb.fh);
 }
 
@@ -440,7 +440,7 @@ static int march_resident_ctas(int fmt) {
     static int cache[4][64];
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || fmt < 0 || fmt > 3) return 152;
+    if (dev < 0 || dev >= 64 || fmt < 0 || fmt > 3) return kSMs;
     int &c = cache[fmt][dev];
     if (c == 0) {
         int sms = 0, nb = 0;

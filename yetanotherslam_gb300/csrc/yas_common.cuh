@@ -24,6 +24,9 @@ constexpr int kBlockSide = 8;      // voxels per block edge (VoxelMap.h:12)
 constexpr int kBlockVoxels = 512;  // voxels per block (VoxelMap.h:13)
 constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr int kMaxProbes = 2048;   // bounded linear probing (no unbounded spin)
+// SMs of a GB300; grid-stride kernels size their grids in multiples of it
+// (their results do not depend on the grid).
+constexpr int kSMs = 152;
 constexpr int kCoordBits = 21;
 constexpr int kCoordMax = (1 << (kCoordBits - 1)) - 1;   // 1048575
 constexpr int kCoordMin = -(1 << (kCoordBits - 1));      // -1048576
