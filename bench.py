@@ -46,6 +46,31 @@ WORKLOAD = {
 }
 
 
+def rank_max(x: float) -> float:
+    """x maximised over the ranks of the current process group (x alone when there
+    is none): NCCL reduces a CUDA tensor, gloo a CPU one."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seeds(rank: int) -> dict:
+    """Seeds of one replica: every rank runs its own session, served sessions and
+    batched submaps on distinct seeded scenes (no data-path exchange)."""
+    return {"scene": WORKLOAD["scene_seed"] + rank, "served": 100 + 1000 * rank, "batched": 7 + 1000 * rank}
+
+
+def whole_job_rate(world: int, units_per_rank: int, max_seconds: float) -> float:
+    """Units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / max_seconds
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -156,7 +181,8 @@ def run_gpu(args):
     W, H = WORKLOAD["width"], WORKLOAD["height"]
     K = synth.intrinsics(W, H)
     nframes = 1 + args.warmup + args.steps
-    frames = make_frames(nframes + 2 * args.profile_frames + 2, W, H, WORKLOAD["scene_seed"] + rank)
+    seeds = replica_seeds(rank)
+    frames = make_frames(nframes + 2 * args.profile_frames + 2, W, H, seeds["scene"])
 
     def new_session():
         return rf.Session(W, H, K, hash_slots=WORKLOAD["hash_slots"], max_blocks=WORKLOAD["max_blocks"],
@@ -193,11 +219,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    total_ms = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = rank_max(float(sum(times)))
     lat = sorted(times)
     kernels = s.kernels_per_frame()
 
@@ -241,19 +263,21 @@ def run_gpu(args):
     for i in range(1, 1 + args.warmup):
         s2.process(pin_rgb[i], pin_dep[i])
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for i in range(1 + args.warmup, nframes):
         s2.process(pin_rgb[i], pin_dep[i])
-    e2e_s = time.perf_counter() - t0
+    e2e_s = rank_max(time.perf_counter() - t0)
     s2.close()
 
     # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
     cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
-    served = run_served(100 + 1000 * rank, args.served_gn) if args.served else None
-    batched = run_batched(7 + 1000 * rank) if args.batched else None
+    served = run_served(seeds["served"], args.served_gn) if args.served else None
+    batched = run_batched(seeds["batched"]) if args.batched else None
     large = run_large(args.large_frames) if args.large else None
 
-    value = world * args.steps / (total_ms * 1e-3)
+    value = whole_job_rate(world, args.steps, total_ms * 1e-3)
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -273,7 +297,7 @@ def run_gpu(args):
                        frame_status_nonzero=int(sum(1 for x in statuses if x != 0)),
                        stage_ms_per_frame={stage_name(k): round(v, 4) for k, v in sorted(per_frame.items())},
                        visible_blocks=nvis),
-        "e2e": {"value": round(world * args.steps / e2e_s, 2), "unit": "frames/s",
+        "e2e": {"value": round(whole_job_rate(world, args.steps, e2e_s), 2), "unit": "frames/s",
                 "h2d_bytes_per_step": W * H * 3 + W * H * 2, "d2h_bytes_per_step": 256},
         "gpu_launches": kernels * args.steps,
         "roofline": {"bound": "hbm", "kernel": stage_name(dom), "achieved": round(achieved, 1), "peak": peak,
