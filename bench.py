@@ -684,7 +684,7 @@ def run_reference(args):
 
     W, H = WORKLOAD["width"], WORKLOAD["height"]
     K = synth.intrinsics(W, H)
-    warm = min(args.warmup, 2)
+    warm = max(3, min(args.warmup, 5))  # at least 3 untimed frames, as the GPU arm
     steps = min(args.steps, args.cpu_frames)
     frames = make_frames(1 + warm + steps, W, H, WORKLOAD["scene_seed"])
     import oracle as orc
