@@ -82,6 +82,35 @@ def test_served_sessions_same_alone_and_in_mix(cuda, per_session):
     assert st["frames"] == len(specs) * n and st["p99_ms"] > 0.0
 
 
+def test_per_session_gn_admission_beyond_co_resident_ctas(cuda):
+    """Ten 640x480 sessions at once: their GN shares (16 CTAs each, 160 in all)
+    exceed the 152 co-resident CTAs, so some frames' GN launches wait for
+    others' to finish.  Every session's poses still equal, bit for bit, its
+    poses served alone."""
+    n, W, H = 4, 640, 480
+    seeds = list(range(21, 31))
+    seqs = [sequence(seed, n, W, H) for seed in seeds]
+    alone = [_serve_alone(seq, W, H, True) for seq in seqs[:3]]
+    srv = serving.Server(hbm_reserve_bytes=1 << 30, gn_per_session=True)
+    sids = [srv.open(W, H, synth.intrinsics(W, H), **MAP) for _ in seeds]
+    for k in range(n):
+        for sid, seq in zip(sids, seqs):
+            rgb, d16, _, _ = seq[k]
+            while srv.submit(sid, rgb, d16) != 0:
+                threading.Event().wait(0.0005)
+    srv.drain()
+    results: dict[int, list] = {}
+    for r in srv.poll(1024):
+        results.setdefault(r["session"], []).append(r)
+    srv.close()
+    assert all(r["status"] == 0 for rs in results.values() for r in rs)
+    for sid, ref in zip(sids[:3], alone):
+        mine = sorted(results[sid], key=lambda r: r["frame"])
+        assert [r["frame"] for r in mine] == list(range(n))
+        for r, T in zip(mine, ref):
+            assert np.array_equal(r["Tcm"], T), (sid, r["frame"])
+
+
 def test_served_matches_standalone_session(cuda):
     W, H, n = 320, 240, 8
     seq = sequence(3, n, W, H)
