@@ -1,6 +1,6 @@
 """Benchmark: tracking + fusion frames/s of one SLAM session on one GB300.
 
-Workload (the BASELINE metric's configuration): 640x480 RGB-D frames of the
+Workload (the headline metric's configuration): 640x480 RGB-D frames of the
 seeded synthetic scene (box room, 20 spheres, 10 cuboids, sigma = 1.5 mm z^2
 depth noise, 1 % dropout), 5 mm voxels, truncation 3 voxels, 2^21 hash
 slots, FP16 TSDF + u8 weight (rounding residual kept), 3-level RGB+ICP pyramid with {10,5,3} GN
@@ -134,7 +134,8 @@ def make_frames(n: int, w: int, h: int, seed: int):
     return [sc.render(i, w, h) for i in range(n)]
 
 
-# algorithmic bytes per launch of each profiled stage
+# algorithmic bytes per launch of each profiled stage: compulsory bytes of one
+# pass over its inputs and outputs (per-pixel and per-block figures below)
 def stage_bytes(stage: int, P: list[int], nvis: int, vbytes: int, P0: int) -> float:
     if 10 <= stage < 20:  # pass A: ref invd+int (8) + cur int/gx/gy (12) + res4 (16) + 4 float4 maps (64)
         return 100.0 * P[stage - 10]
