@@ -4,7 +4,10 @@ Reference behaviour: RGBDFusion/src/VoxelMap.cu:173-199 (Swap), 213-444
 (CreateBlockFunctor, MapStructFusionFunctor, Fuse(MapStruct*)), 446-515
 (Reserve).  Bars:
   * block coordinate set after fusion: bit-exact (FP32 canonical allocation);
-  * weights: exact; TSDF within 1e-5 of the truncation (F32 storage);
+  * weights: exact; TSDF within 1e-5 of the truncation (F32 storage); with
+    the reference's int16 storage (S16, the oracle keeping the same storage)
+    within four int16 steps: each source map within two, plus one truncation
+    of the blend;
   * reserve keeps every block's contents bit for bit;
   * de-integrating a frame matches the oracle's de-integration (weights exact,
     TSDF within 1e-5) and, on the blocks that existed when the frame was
@@ -25,15 +28,15 @@ pytestmark = pytest.mark.gpu
 VS = 0.008
 
 
-def _maps(K, slots=1 << 18, blocks=1 << 15):
+def _maps(K, slots=1 << 18, blocks=1 << 15, fmt=rf.VOXEL_F32):
     m = rf.MapStruct(K)
-    m.create_config(slots, blocks, VS, 3 * VS, rf.VOXEL_F32)
-    return m, oracle.Map(VS, 3 * VS)
+    m.create_config(slots, blocks, VS, 3 * VS, fmt)
+    return m, oracle.Map(VS, 3 * VS, int16_sdf=fmt == rf.VOXEL_S16)
 
 
-def _build(seq, frames, K, T_map, slots=1 << 18, blocks=1 << 15):
+def _build(seq, frames, K, T_map, slots=1 << 18, blocks=1 << 15, fmt=rf.VOXEL_F32):
     """Submap with pose T_map (world), fused from `frames` of `seq`."""
-    m, o = _maps(K, slots, blocks)
+    m, o = _maps(K, slots, blocks, fmt)
     m.SetPose(T_map)
     Tinv = np.linalg.inv(T_map)
     for i in frames:
@@ -53,16 +56,17 @@ def _compare(m, o, tol=1e-5):
     return cg.shape[0]
 
 
-def test_fuse_map_matches_oracle(cuda):
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_S16])
+def test_fuse_map_matches_oracle(cuda, fmt):
     W, H = 320, 240
     K = synth.intrinsics(W, H)
     seq = sequence(21, 8, W, H)
     TA, TB = seq[0][3], seq[4][3]
-    ma, oa = _build(seq, range(0, 4), K, TA)
-    mb, ob = _build(seq, range(4, 8), K, TB)
+    ma, oa = _build(seq, range(0, 4), K, TA, fmt=fmt)
+    mb, ob = _build(seq, range(4, 8), K, TB, fmt=fmt)
     ma.FuseMap(mb)
     assert not oa.fuse_map(ob, TA, TB)
-    n = _compare(ma, oa)
+    n = _compare(ma, oa, tol=1e-5 if fmt == rf.VOXEL_F32 else 4.0 / 32767)
     assert n > 0 and mb.Empty()
 
 

@@ -274,7 +274,7 @@ def test_reset_clears_map(cuda):
     assert m.num_allocated() == o.num_blocks
 
 
-@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16])
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_F16, rf.VOXEL_S16])
 def test_submap_file_roundtrip(cuda, fmt, tmp_path):
     """SaveToFile / ReadFromFile: the round trip is bit-exact, the loaded map
     (grown from a small capacity) fuses on exactly as the original, a format
