@@ -86,30 +86,40 @@ class ClockSampler:
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int = 0):
+    def __init__(self, index: int = 0, period_ms: int = 50):
         self.index = index
+        self.period_ms = period_ms
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi in loop mode (a sample every period_ms) for the whole region
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", str(self.period_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.strip().split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        time.sleep(0.15)  # the first sample lands before the timed region starts
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
+        time.sleep(self.period_ms * 1e-3)  # and one after it ends
+        if self._proc is not None:
+            self._proc.terminate()  # the process this sampler started, by its handle
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         if self._t:
             self._t.join(timeout=10)
 
