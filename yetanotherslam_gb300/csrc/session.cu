@@ -227,19 +227,22 @@ static void enqueue_pre(yas_session *s) {
     yas_tracker *tr = s->tr;
     cudaStream_t st = s->stream;
     if (s->side && !s->profiling) {
-        // the two branches touch disjoint buffers: run them side by side
+        // the two branches touch disjoint buffers: run them side by side; the
+        // GN state reset (it reads neither branch's outputs) ends the shorter
+        // frame branch, off the raycast's path
         cudaEventRecord(s->ev_fork, st);
         cudaStreamWaitEvent(s->side, s->ev_fork, 0);
         enqueue_raycast_branch(s, s->side);
         enqueue_frame_branch(s, st);
+        launch_gn_init(tr, pose_identity(), st);
         cudaEventRecord(s->ev_join, s->side);
         cudaStreamWaitEvent(st, s->ev_join, 0);
     } else {
         enqueue_frame_branch(s, st);
         enqueue_raycast_branch(s, st);
+        prof_mark(s, kStGnInit);
+        launch_gn_init(tr, pose_identity(), st);
     }
-    prof_mark(s, kStGnInit);
-    launch_gn_init(tr, pose_identity(), st);
 }
 
 // A tracked frame after the Gauss-Newton schedule: pose update, fusion, frame
