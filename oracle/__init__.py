@@ -221,11 +221,14 @@ class Tracker:
 class Session:
     def __init__(self, w: int, h: int, K, voxel_size: float, trunc: float, levels: int = 3,
                  iters=(10, 5, 3, 3, 3), mode: int = 3, depth_scale: float = 0.001, max_step: float = 0.1,
-                 kind: str = "f64"):
+                 kind: str = "f64", int16_sdf: bool = False):
+        """int16_sdf: the session's map keeps the reference's int16 storage."""
         self.L = lib(kind)
         it = np.ascontiguousarray(np.asarray(list(iters) + [0] * (5 - len(iters)), dtype=np.int32)[:5])
         self.hdl = self.L.orc_session_create(w, h, _ptr(_kvec(K)), voxel_size, trunc, levels, _ptr(it), mode,
                                              depth_scale, max_step)
+        if int16_sdf:
+            self.L.orc_map_set_storage(self.L.orc_session_map(self.hdl), 1)
         self.w, self.h = w, h
         self.K = K
 

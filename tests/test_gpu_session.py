@@ -1,8 +1,9 @@
 """End-to-end session parity: the captured per-frame pipeline against the
 oracle's restatement of Tracking::TrackRGBD's dense calls
 (FullSystem/src/Tracking.cpp:139-197).  Bars: every frame pose within
-1e-4 m and 1e-4 rad of the oracle's; graph and eager execution bit-identical;
-the fused block set equal to the oracle's.
+1e-4 m and 1e-4 rad of the oracle's (FP32 storage; and the reference's int16
+storage against the oracle keeping the same storage); graph and eager
+execution bit-identical; the fused block set equal to the oracle's.
 """
 from __future__ import annotations
 
@@ -30,11 +31,12 @@ def _run(W, H, n, fmt, use_graph, seed=3, vs=0.008):
     return s, poses
 
 
-def test_session_poses_match_oracle(cuda):
+@pytest.mark.parametrize("fmt", [rf.VOXEL_F32, rf.VOXEL_S16])
+def test_session_poses_match_oracle(cuda, fmt):
     W, H, n = 320, 240, 12
-    s, poses = _run(W, H, n, rf.VOXEL_F32, True)
+    s, poses = _run(W, H, n, fmt, True)
     K = synth.intrinsics(W, H)
-    o = oracle.Session(W, H, K, 0.008, 0.024)
+    o = oracle.Session(W, H, K, 0.008, 0.024, int16_sdf=fmt == rf.VOXEL_S16)
     seq = sequence(3, n, W, H)
     gt = rel_poses(seq)
     for i, (rgb, d16, _, _) in enumerate(seq):
