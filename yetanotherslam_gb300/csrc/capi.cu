@@ -890,8 +890,8 @@ YAS_API int yas_raycaster_create(yas_raycaster **out, int width, int height, con
     rc->rb.zw = (width + 7) / 8;
     rc->rb.zh = (height + 7) / 8;
     const size_t nz = (size_t)rc->rb.zw * rc->rb.zh;
-    rc->rb.fw = (width + 3) / 4;
-    rc->rb.fh = (height + 3) / 4;
+    rc->rb.fw = (width + (1 << kFineShift) - 1) >> kFineShift;
+    rc->rb.fh = (height + (1 << kFineShift) - 1) >> kFineShift;
     if (cudaMalloc(&rc->rb.znear, nz * 4) != cudaSuccess || cudaMalloc(&rc->rb.zfar, nz * 4) != cudaSuccess ||
         cudaMalloc(&rc->rb.queue, sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc(&rc->rb.fnear, (size_t)rc->rb.fw * rc->rb.fh * 4) != cudaSuccess ||

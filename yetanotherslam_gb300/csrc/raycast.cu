@@ -91,10 +91,11 @@ __global__ void __launch_bounds__(128) zrange_fill_kernel(MapDev m, Cam cam, con
         if (zmax >= m.depth_min) {
             int fx0 = 0, fy0 = 0, fx1 = fw - 1, fy1 = fh - 1;
             if (!behind) {
-                fx0 = max(fx0, clamp_floor((pu0 - 1.0f) * 0.25f));
-                fy0 = max(fy0, clamp_floor((pv0 - 1.0f) * 0.25f));
-                fx1 = min(fx1, clamp_floor((pu1 + 1.0f) * 0.25f));
-                fy1 = min(fy1, clamp_floor((pv1 + 1.0f) * 0.25f));
+                constexpr float kInvCell = 1.0f / (float)(1 << kFineShift);
+                fx0 = max(fx0, clamp_floor((pu0 - 1.0f) * kInvCell));
+                fy0 = max(fy0, clamp_floor((pv0 - 1.0f) * kInvCell));
+                fx1 = min(fx1, clamp_floor((pu1 + 1.0f) * kInvCell));
+                fy1 = min(fy1, clamp_floor((pv1 + 1.0f) * kInvCell));
             }
             const int fz = __float_as_int(fmaxf(fminf(zmin, m.depth_max), 0.0f));
             for (int y = fy0; y <= fy1; ++y)
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(32 * WX * WY) march_kernel(MapDev m, Cam cam, 
         const float rstep = m.trunc / m.voxel_size;
         RayState R;
         if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)), __ldg(zfar + (y >> 3) * zw + (x >> 3)),
-                      __ldg(fnear + (y >> 2) * fw + (x >> 2)), x, y, R)) {
+                      __ldg(fnear + (y >> kFineShift) * fw + (x >> kFineShift)), x, y, R)) {
             VoxelReader<FMT> rd(m);
             while (!ray_step(rd, rstep, R)) {
             }
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(128) march_persistent_kernel(MapDev m, Cam cam
                     y = (t / tiles_x) * 4 + (l >> 3);
                     if (x < cam.w && y < cam.h) {
                         if (ray_setup(cam, P->T, vsinv, __ldg(znear + (y >> 3) * zw + (x >> 3)),
-                                      __ldg(zfar + (y >> 3) * zw + (x >> 3)), __ldg(fnear + (y >> 2) * fw + (x >> 2)),
+                                      __ldg(zfar + (y >> 3) * zw + (x >> 3)), __ldg(fnear + (y >> kFineShift) * fw + (x >> kFineShift)),
                                       x, y, R))
                             active = true;
                         else

@@ -27,6 +27,8 @@ constexpr int kMaxProbes = 2048;   // bounded linear probing (no unbounded spin)
 // SMs of a GB300; grid-stride kernels size their grids in multiples of it
 // (their results do not depend on the grid).
 constexpr int kSMs = 152;
+// Fine near-bound cells of the ray march: 2^kFineShift pixels square.
+constexpr int kFineShift = 2;
 constexpr int kCoordBits = 21;
 constexpr int kCoordMax = (1 << (kCoordBits - 1)) - 1;   // 1048575
 constexpr int kCoordMin = -(1 << (kCoordBits - 1));      // -1048576
