@@ -340,7 +340,7 @@ def _pingpong(k: int, n: int) -> int:
     return k if k < n else period - k
 
 
-def run_served(seed: int = 100, gn_per_session: bool | None = None):
+def run_served(seed: int = 100, gn_per_session: bool | None = None, gn_pixels_per_cta: int = 0):
     """C4: 32 concurrent sessions (half 640x480, half 320x240, distinct seeded scenes), Poisson
     arrivals at 30 Hz per session, through the request server; then the same sessions saturated
     (every session resubmits as soon as its ring has room); then the plain FP32 per-frame form
@@ -357,7 +357,7 @@ def run_served(seed: int = 100, gn_per_session: bool | None = None):
         W, H = cfg["resolutions"][i % 2]
         sessions.append((W, H, make_frames(n_r, W, H, seed + i)))
     srv = serving.Server(max_sessions=cfg["sessions"], hbm_reserve_bytes=8 << 30, ring_frames=8,
-                         gn_per_session=gn_per_session)
+                         gn_per_session=gn_per_session, gn_pixels_per_cta=gn_pixels_per_cta)
     sids = []
     for W, H, _ in sessions:
         sids.append(srv.open(W, H, synth.intrinsics(W, H), hash_slots=cfg["hash_slots"][f"{W}x{H}"],
@@ -736,6 +736,8 @@ def main():
     ap.add_argument("--served", type=int, default=1, help="1: also measure 32 served sessions (C4)")
     ap.add_argument("--served-gn", type=lambda v: bool(int(v)), default=None,
                     help="served sessions: 1 = a GN launch per session (the server's default), 0 = gathered")
+    ap.add_argument("--served-ppc", type=int, default=0,
+                    help="served sessions, GN per session: level-0 pixels per CTA of a session's share (0: default)")
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
     ap.add_argument("--large", type=int, default=0, help="1: also run the 2000-frame 1280x720 large map (C5)")
     ap.add_argument("--large-frames", type=int, default=2000)
@@ -745,7 +747,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.leg:
-        fn = {"served": lambda: run_served(100, args.served_gn), "batched": lambda: run_batched(7),
+        fn = {"served": lambda: run_served(100, args.served_gn, args.served_ppc), "batched": lambda: run_batched(7),
               "batched-pass": lambda: run_batched(7, only_pass=True),
               "large": lambda: run_large(args.large_frames)}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn()}))

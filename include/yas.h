@@ -535,6 +535,9 @@ typedef struct yas_server_config {
                                * (a fixed CTA share) on its session's stream at   *
                                * once; 0: sessions whose first half is queued     *
                                * gather into one batched launch                   */
+    int gn_pixels_per_cta;    /* gn_per_session: a session's GN share is one CTA per *
+                               * this many level-0 pixels, at most 32 CTAs (0: the *
+                               * default, 16384)                                   */
 } yas_server_config;
 
 typedef struct yas_served_result {

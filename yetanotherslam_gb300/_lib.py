@@ -55,7 +55,7 @@ class SessionConfig(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_sessions", C.c_int), ("hbm_reserve_bytes", C.c_size_t), ("ring_frames", C.c_int),
-                ("gn_per_session", C.c_int)]
+                ("gn_per_session", C.c_int), ("gn_pixels_per_cta", C.c_int)]
 
 
 class BatchTuning(C.Structure):

@@ -188,14 +188,18 @@ int launch_pre_frame(ServedSession *ss) {
     return YAS_OK;
 }
 
-// CTA share of a session's own GN launch: 16 K pixels of level 0 per CTA.
+// CTA share of a session's own GN launch: by default one CTA per 16 K pixels
+// of level 0, at most kOwnMaxCtas.
 constexpr int kOwnPixelsPerCta = 16384;
+constexpr int kOwnMaxCtas = 32;
 
 // gn_per_session: the frame's own GN launch right after its first half, then
 // its second half, all on the session's stream.  The descriptor of each frame
 // parity names the tracker's fixed buffers, so it is built once.
 int own_share(yas_server *srv, ServedSession *ss) {
-    return std::min(srv->capacity, gn_batch_ctas(session_tracker(ss->s), kOwnPixelsPerCta));
+    const long long ppc = srv->cfg.gn_pixels_per_cta > 0 ? srv->cfg.gn_pixels_per_cta : kOwnPixelsPerCta;
+    const long long n = ((long long)ss->w * ss->h + ppc - 1) / ppc;
+    return (int)std::min<long long>(std::min(srv->capacity, kOwnMaxCtas), std::max(1LL, n));
 }
 
 int launch_own_gn(yas_server *srv, ServedSession *ss) {
@@ -348,6 +352,7 @@ YAS_API int yas_server_config_default(yas_server_config *cfg) {
     cfg->hbm_reserve_bytes = (size_t)4 << 30;
     cfg->ring_frames = 4;
     cfg->gn_per_session = 1;
+    cfg->gn_pixels_per_cta = 0;
     return YAS_OK;
 }
 

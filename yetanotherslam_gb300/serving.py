@@ -18,7 +18,7 @@ from .rgbdfusion import session_config
 
 class Server:
     def __init__(self, max_sessions: int = 64, hbm_reserve_bytes: int = 4 << 30, ring_frames: int = 4,
-                 gn_per_session: bool | None = None):
+                 gn_per_session: bool | None = None, gn_pixels_per_cta: int = 0):
         cfg = L.ServerConfig()
         L.call("yas_server_config_default", C.byref(cfg))
         cfg.max_sessions = max_sessions
@@ -26,6 +26,7 @@ class Server:
         cfg.ring_frames = ring_frames
         if gn_per_session is not None:
             cfg.gn_per_session = int(bool(gn_per_session))
+        cfg.gn_pixels_per_cta = int(gn_pixels_per_cta)
         self.handle = C.c_void_p()
         L.call("yas_server_create", C.byref(self.handle), C.byref(cfg))
         self._sizes: dict[int, tuple[int, int]] = {}
