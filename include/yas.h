@@ -304,18 +304,24 @@ typedef struct yas_gn_level {
  * callers that must not allocate device memory: a host that owns the whole
  * device-memory budget of the process, or code that runs where an allocation
  * would synchronise the device or is not allowed (inside a real-time frame
- * callback, during another component's stream capture).  It allocates
- * nothing: its scratch (per-pixel residuals, per-CTA partial sums, tickets
- * and the solver state) is a fixed array of about 5.3 MB in the library's
- * static device memory, present on every device that loads the library.
+ * callback).  It allocates nothing: its scratch (per-pixel residuals, per-CTA
+ * partial sums, tickets and the solver state) is a fixed array of about
+ * 5.3 MB in the library's static device memory, present on every device that
+ * loads the library until the process exits.
  * Limits: width * height <= 640 * 480 and width, height >= 4; larger levels
- * return YAS_ERR_CAPACITY.  mode: enum yas_track_mode.  dev_out (device,
- * 46 doubles): H row-major (36), b (6), stats (4) as yas_tracker_compute_step.
- * The first call on a device resolves the scratch address (no allocation);
- * make that first call before capturing a stream.  All calls share the one
- * scratch array, so calls whose GPU work overlaps (other streams, other host
- * threads) race and must be serialised by the caller; the call itself only
- * enqueues work on `stream` (NULL: legacy default stream). */
+ * return YAS_ERR_CAPACITY before any work is enqueued.  mode: enum
+ * yas_track_mode.  dev_out (device, 46 doubles): H row-major (36), b (6),
+ * stats (4) as yas_tracker_compute_step.  The sums are always the compensated
+ * reduction (TwoSum FP32 partial sums, FP64 totals), whatever
+ * yas_tracker_set_reduction chose for any tracker; with that reduction the
+ * result is bit-identical to yas_tracker_compute_step's for the same maps.
+ * The first call on a device, and the first after the device's context
+ * changes (e.g. after cudaDeviceReset), resolves the scratch address (no
+ * allocation); make that call before capturing a stream.  All calls share the
+ * one scratch array, which keeps the last call's contents (the call clears
+ * what must start at zero), so calls whose GPU work overlaps (other streams,
+ * other host threads) race and must be serialised by the caller; the call
+ * itself only enqueues work on `stream` (NULL: legacy default stream). */
 YAS_API int yas_gn_linearise_static(const yas_gn_level *level, const yas_pose *T, int mode, double *dev_out,
                                     void *stream);
 

@@ -7,17 +7,23 @@
  *
  * Parity status: the reference's dense path cannot be compiled here (it
  * needs OpenCV with CUDA modules, Eigen and Sophus, none of which is
- * installed) and its repository ships no tests, golden vectors or fixtures
- * for this path, so this restatement is pinned by the analytic known-answer
- * tests under tests/ (plane and sphere TSDFs, exact plane raycasts, sphere
- * meshes, known-motion recovery) and not by outputs of the reference itself:
- * parity unpinned against the reference.
+ * installed) and its repository ships no tests or golden vectors for this
+ * path.  The one piece of reference data on the path, its marching-cubes
+ * table (RGBDFusion/utils/TriangleTable.h), pins this restatement's table
+ * generator (edge masks, triangle counts and oriented polygons of every
+ * case; tests/test_mc_reference_topology.py).  Everything else is pinned by
+ * the analytic known-answer tests under tests/ (plane and sphere TSDFs,
+ * exact plane raycasts, sphere meshes, known-motion recovery), not by
+ * outputs of the reference itself.
  *
  * Precision: every discrete decision the reference makes from FP32 geometry
  * (block allocation along each ray, block visibility, the pixel a voxel
- * projects to, the truncation gate, z-range tile coverage) is evaluated in
- * IEEE FP32 with one rounding per operation in a fixed order (build with
- * -ffp-contract=off), exactly as the CUDA path does; continuous quantities
+ * projects to, the truncation gate, z-range tile coverage; in the tracker,
+ * the reference pixels that project inside the current image, the ICP
+ * pairs and gates at the FP32 pose, and GetTransform's FP32 error and its
+ * keep-the-better-estimate comparison) is evaluated in IEEE FP32 with one
+ * rounding per operation in a fixed order (build with -ffp-contract=off),
+ * exactly as the CUDA path does; continuous quantities
  * (TSDF accumulation, ray marching, image pyramids, residuals, reductions,
  * the 6x6 solve and the SE(3) update) use `real`, which is double in the
  * checker build (liboracle64) and float in the multi-threaded CPU-baseline

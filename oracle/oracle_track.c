@@ -404,6 +404,84 @@ static real bilinear(const float *m, int w, real x, real y) {
     return ((real)r0[0] * (1 - cx) + (real)r0[1] * cx) * (1 - cy) + ((real)r1[0] * (1 - cx) + (real)r1[1] * cx) * cy;
 }
 
+/* Discrete decisions of the tracker, in IEEE FP32 at the FP32 pose Tf (the
+ * reference casts its SE3d to float for the kernels), one rounding per
+ * operation in the device code's fixed order: which reference pixels
+ * project inside the current image (se3StepRGBFunctor's bounds,
+ * TrackingUtils.h:73-150), which model point pairs with which current pixel
+ * and passes the ICP gates (IcpStepFunctor::ProjectPoint,
+ * RGBDTracking.cu:326-358), and the point-to-plane residual whose squares
+ * GetTransform's error sums.  Coordinates are tested as floats before they
+ * are converted, so NaN and infinite projections are outside. */
+static float dot3f(float a0, float a1, float a2, float b0, float b1, float b2) {
+    const float p0 = a0 * b0, p1 = a1 * b1, p2 = a2 * b2;
+    const float s = p0 + p1;
+    return s + p2;
+}
+
+/* R K^-1 in FP32 from the FP32 pose (the device forms it the same way). */
+static void rkinv_f(const float *Tf, const lcam *c, float *RK) {
+    const float cxi = c->cx * c->invfx, cyi = c->cy * c->invfy;
+    for (int i = 0; i < 3; ++i) {
+        RK[i * 3 + 0] = Tf[i * 4 + 0] * c->invfx;
+        RK[i * 3 + 1] = Tf[i * 4 + 1] * c->invfy;
+        const float a = Tf[i * 4 + 0] * cxi, bq = Tf[i * 4 + 1] * cyi;
+        const float d = Tf[i * 4 + 2] - a;
+        RK[i * 3 + 2] = d - bq;
+    }
+}
+
+/* Reference pixel (x, y) at depth z warped by Tf (TransformReferencePoint,
+ * ImageProc.cu:42-78): (RK (x, y, 1)) z + t. */
+static void warp_f(const float *RK, const float *Tf, int x, int y, float z, float *p) {
+    const float fx = (float)x, fy = (float)y;
+    for (int i = 0; i < 3; ++i) {
+        const float a = RK[i * 3] * fx, bq = RK[i * 3 + 1] * fy;
+        const float s = a + bq;
+        const float s2 = s + RK[i * 3 + 2];
+        const float m = s2 * z;
+        p[i] = m + Tf[i * 4 + 3];
+    }
+}
+
+static int rgb_project_f(const lcam *c, const float *p, float *u, float *v) {
+    const float ax = c->fx * p[0], ay = c->fy * p[1];
+    const float qx = ax / p[2], qy = ay / p[2];
+    *u = qx + c->cx;
+    *v = qy + c->cy;
+    return *u > 0.0f && *v > 0.0f && *u < (float)(c->w - 1) && *v < (float)(c->h - 1);
+}
+
+/* Model pixel k: returns the current pixel index it pairs with and passes
+ * the gates, or -1; rf = n . (v_c - v_m) in FP32. */
+static int icp_match_f(const orc_tracker *t, const lcam *c, const lbufs *cb, const lbufs *rb, const float *Tf, int k,
+                       float *rf) {
+    const float *vm = rb->vmap + (size_t)k * 4;
+    if (!(vm[3] >= 0.0f)) return -1;
+    float vl[3], nl[3];
+    for (int i = 0; i < 3; ++i) vl[i] = dot3f(Tf[i * 4], Tf[i * 4 + 1], Tf[i * 4 + 2], vm[0], vm[1], vm[2]) + Tf[i * 4 + 3];
+    const float invz = 1.0f / vl[2];
+    const float ax = c->fx * vl[0], ay = c->fy * vl[1];
+    const float bx = ax * invz, by = ay * invz;
+    const float cxs = bx + c->cx, cys = by + c->cy;
+    const float fu = floorf(cxs + 0.5f), fv = floorf(cys + 0.5f);
+    if (!(fu >= 0.0f && fv >= 0.0f && fu < (float)c->w && fv < (float)c->h)) return -1;
+    const int q = (int)fv * c->w + (int)fu;
+    const float *vc = cb->vmap + (size_t)q * 4;
+    if (!(vc[3] >= 0.0f)) return -1;
+    const float *nm = rb->nmap + (size_t)k * 4, *nc = cb->nmap + (size_t)q * 4;
+    for (int i = 0; i < 3; ++i) nl[i] = dot3f(Tf[i * 4], Tf[i * 4 + 1], Tf[i * 4 + 2], nm[0], nm[1], nm[2]);
+    const float dx = vl[0] - vc[0], dy = vl[1] - vc[1], dz = vl[2] - vc[2];
+    const float dist = sqrtf(dot3f(dx, dy, dz, dx, dy, dz));
+    const float a0 = nc[1] * nl[2], a1 = nc[2] * nl[1], b0 = nc[2] * nl[0], b1 = nc[0] * nl[2];
+    const float c0 = nc[0] * nl[1], c1 = nc[1] * nl[0];
+    const float cx_ = a0 - a1, cy_ = b0 - b1, cz_ = c0 - c1;
+    const float angle = sqrtf(dot3f(cx_, cy_, cz_, cx_, cy_, cz_));
+    if (!(angle < t->angle_th && dist <= t->dist_th && nm[3] > 0 && nc[3] > 0)) return -1;
+    *rf = dot3f(nl[0], nl[1], nl[2], vc[0] - vl[0], vc[1] - vl[1], vc[2] - vl[2]);
+    return q;
+}
+
 /* One linearisation at T on level l: sums[0..27] ICP products (27 = r^2),
  * sums[28] ICP count; rgb[0..27] weighted photometric products, rgbn count;
  * returns huber threshold. */
@@ -411,6 +489,9 @@ static void linearise(orc_tracker *t, int l, const double *T, double *H, double 
     const lcam *c = &t->cam[l];
     const lbufs *cb = &t->set[t->cur][l], *rb = &t->set[1 - t->cur][l];
     const int n = c->w * c->h;
+    float Tf[12], RKf[9];
+    for (int i = 0; i < 12; ++i) Tf[i] = (float)T[i];
+    rkinv_f(Tf, c, RKf);
     /* R K^-1 (TransformReferencePoint, ImageProc.cu:86-101) */
     double RK[9];
     for (int i = 0; i < 3; ++i) {
@@ -432,15 +513,19 @@ static void linearise(orc_tracker *t, int l, const double *T, double *H, double 
             int ok = 0;
             const float zinv = rb->invd[k];
             if (zinv > 0.0f) {
-                const real z = (real)(1.0f / zinv);
+                const float zf = 1.0f / zinv;
+                const real z = (real)zf;
                 real p[3];
                 for (int i = 0; i < 3; ++i) p[i] = (RK[i * 3] * x + RK[i * 3 + 1] * y + RK[i * 3 + 2]) * z + T[i * 4 + 3];
                 pts[3 * k] = p[0];
                 pts[3 * k + 1] = p[1];
                 pts[3 * k + 2] = p[2];
-                const real u = (real)c->fx * p[0] / p[2] + (real)c->cx;
-                const real v = (real)c->fy * p[1] / p[2] + (real)c->cy;
-                if (u > 0 && v > 0 && u < c->w - 1 && v < c->h - 1) {
+                /* inside or outside, and where the current image is sampled:
+                 * the FP32 decision at Tf */
+                float pf[3], uf, vf;
+                warp_f(RKf, Tf, x, y, zf, pf);
+                if (rgb_project_f(c, pf, &uf, &vf)) {
+                    const real u = (real)uf, v = (real)vf;
                     r = bilinear(cb->inten, c->w, u, v) - (real)rb->inten[k];
                     gx = bilinear(t->gx[l], c->w, u, v);
                     gy = bilinear(t->gy[l], c->w, u, v);
@@ -488,23 +573,15 @@ static void linearise(orc_tracker *t, int l, const double *T, double *H, double 
     if (do_icp) {
         /* IcpStepFunctor (RGBDTracking.cu:432-488) */
         for (int k = 0; k < n; ++k) {
+            /* the pairing and the gates: the FP32 decision at Tf */
+            float rf = 0.0f;
+            const int q = icp_match_f(t, c, cb, rb, Tf, k, &rf);
+            if (q < 0) continue;
             const float *vm = rb->vmap + (size_t)k * 4;
-            if (vm[3] < 0) continue;
+            const float *vc = cb->vmap + (size_t)q * 4, *nm = rb->nmap + (size_t)k * 4;
             real vl[3], nl[3];
             for (int i = 0; i < 3; ++i) vl[i] = T[i * 4] * vm[0] + T[i * 4 + 1] * vm[1] + T[i * 4 + 2] * vm[2] + T[i * 4 + 3];
-            const real invz = 1 / vl[2];
-            const int u = (int)floor((real)c->fx * vl[0] * invz + (real)c->cx + 0.5);
-            const int v = (int)floor((real)c->fy * vl[1] * invz + (real)c->cy + 0.5);
-            if (u < 0 || v < 0 || u >= c->w || v >= c->h) continue;
-            const float *vc = cb->vmap + ((size_t)v * c->w + u) * 4;
-            if (vc[3] < 0) continue;
-            const float *nm = rb->nmap + (size_t)k * 4, *nc = cb->nmap + ((size_t)v * c->w + u) * 4;
             for (int i = 0; i < 3; ++i) nl[i] = T[i * 4] * nm[0] + T[i * 4 + 1] * nm[1] + T[i * 4 + 2] * nm[2];
-            const real d[3] = {vl[0] - vc[0], vl[1] - vc[1], vl[2] - vc[2]};
-            const real dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-            const real cr[3] = {nc[1] * nl[2] - nc[2] * nl[1], nc[2] * nl[0] - nc[0] * nl[2], nc[0] * nl[1] - nc[1] * nl[0]};
-            const real angle = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-            if (!(angle < t->angle_th && dist <= t->dist_th && nm[3] > 0 && nc[3] > 0)) continue;
             real row[7];
             row[0] = nl[0];
             row[1] = nl[1];
@@ -513,9 +590,12 @@ static void linearise(orc_tracker *t, int l, const double *T, double *H, double 
             row[4] = vl[2] * nl[0] - vl[0] * nl[2];
             row[5] = vl[0] * nl[1] - vl[1] * nl[0];
             row[6] = nl[0] * (vc[0] - vl[0]) + nl[1] * (vc[1] - vl[1]) + nl[2] * (vc[2] - vl[2]);
-            int q = 0;
+            int qq = 0;
             for (int i = 0; i < 7; ++i)
-                for (int j = i; j < 7; ++j) icp[q++] += row[i] * row[j];
+                for (int j = i; j < 7; ++j, ++qq)
+                    if (qq < 27) icp[qq] += row[i] * row[j];
+            /* the error's sum of squares: the FP32 residual's rounded squares */
+            icp[27] += (double)(rf * rf);
             icp[28] += 1;
         }
     }
@@ -566,11 +646,13 @@ int orc_tracker_get_transform(orc_tracker *t, const double *init, int swap, doub
     memcpy(est, init, sizeof(est));
     memcpy(best, init, sizeof(best));
     for (int l = t->L - 1; l >= 0; --l) {
-        double last_error = FLT_MAX;
+        float last_error = FLT_MAX;
         for (int it = 0; it < t->iters[l]; ++it) {
             double H[36], b[6], st[4], upd[6], E[12];
             linearise(t, l, est, H, b, st);
-            const double error = sqrt(st[0]) / (st[1] + 6.0);
+            /* float error = sqrt(residualSum) / (numResidual + 6), in FP32 as
+             * the reference computes and compares it */
+            const float error = sqrtf((float)st[0]) / ((float)st[1] + 6.0f);
             orc_ldlt_solve6(H, b, upd);
             if (isnan(upd[0])) {
                 ident34(out);

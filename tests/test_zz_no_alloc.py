@@ -3,13 +3,18 @@
 Some callers of this library cannot allocate device memory: a host
 application that keeps the whole device-memory budget of its process, or code
 running where cudaMalloc would synchronise the device or is not permitted
-(a real-time frame callback, another component's stream capture).  This
-entry point takes the tracker's level maps and an output buffer from the
-caller and keeps its own scratch in fixed static device memory.  These tests
-call it through the C ABI and check it against yas_tracker_compute_step,
-which computes the same linearisation with handle-owned scratch, with the
-tracker parity tests' tolerance (1e-3 of max|H| and max|b|), on two calls in
-a row, since all calls share (and overwrite) the one scratch array.
+(a real-time frame callback).  This entry point takes the tracker's level
+maps and an output buffer from the caller and keeps its own scratch in fixed
+static device memory.  These tests call it through the C ABI, on two calls in
+a row, since all calls share (and overwrite) the one scratch array, and check:
+
+  * bit-identical H, b and statistics against yas_tracker_compute_step, which
+    runs the same passes on the same grid with handle-owned scratch (the
+    level intrinsics used here are exact in FP32, so both paths see the same
+    camera constants);
+  * the oracle's compute_step at the tracker parity tests' tolerance (every
+    entry of H and b within 1e-3 of max|H|, max|b|);
+  * that a warm call leaves the device's free memory unchanged.
 
 The file name makes pytest collect it after every other test file.
 """
@@ -20,6 +25,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import oracle
 from tests.helpers import rel_poses, sequence
 from yetanotherslam_gb300 import _lib as L
 from yetanotherslam_gb300 import rgbdfusion as rf
@@ -44,8 +50,14 @@ def _tracker(mode, W=320, H=240):
     tr.SetTrackingImage(g1)
     tr.SetTrackingDepth(seq[1][2])
     tr.SetReferenceModel(rc.GetVMap())
+    ot = oracle.Tracker(W, H, K, levels=3, iters=(10, 5, 3), mode=mode)
+    ot.set_image(g0, True)
+    ot.set_depth(seq[0][2], True)
+    ot.set_image(g1, False)
+    ot.set_depth(seq[1][2], False)
+    ot.set_model(rc.GetVMap().numpy())
     gt = np.linalg.inv(rel_poses(seq)[1])
-    return tr, (fx, fy, cx, cy), gt, (m, rc)
+    return tr, ot, (fx, fy, cx, cy), gt, (m, rc)
 
 
 def _level(tr, lvl, K):
@@ -61,7 +73,7 @@ def _level(tr, lvl, K):
 def test_static_linearisation_matches_handle_path_twice(cuda, mode):
     import torch
 
-    tr, K, gt, keep = _tracker(mode)
+    tr, ot, K, gt, keep = _tracker(mode)
     out = torch.zeros(46, dtype=torch.float64, device="cuda")
     perturb = np.eye(4)
     perturb[:3, 3] = [0.003, -0.002, 0.001]
@@ -69,15 +81,35 @@ def test_static_linearisation_matches_handle_path_twice(cuda, mode):
         lv = _level(tr, lvl, K)
         for T in (gt, perturb @ gt):
             Hh, bh, sh = tr.compute_step(lvl, T)
+            Ho, bo, so = ot.compute_step(lvl, T)
             for _ in range(2):  # two calls in a row share the static scratch
-                out.zero_()
+                out.fill_(np.nan)
                 L.call("yas_gn_linearise_static", C.byref(lv), C.byref(L.pose_from(T)), mode, out.data_ptr(), None)
                 torch.cuda.synchronize()
                 o = out.cpu().numpy()
                 Hs, bs, ss = o[:36].reshape(6, 6), o[36:42], o[42:46]
-                assert np.abs(Hs - Hh).max() <= 1e-3 * np.abs(Hh).max()
-                assert np.abs(bs - bh).max() <= 1e-3 * max(np.abs(bh).max(), 1e-9)
-                assert abs(ss[1] - sh[1]) <= 2 + 1e-3 * sh[1]
+                assert np.array_equal(Hs, Hh), (lvl, np.abs(Hs - Hh).max())
+                assert np.array_equal(bs, bh), (lvl, np.abs(bs - bh).max())
+                assert np.array_equal(ss, sh, equal_nan=True), (lvl, ss, sh)  # stats[2] is NaN without RGB
+                assert np.abs(Hs - Ho).max() <= 1e-3 * np.abs(Ho).max()
+                assert np.abs(bs - bo).max() <= 1e-3 * max(np.abs(bo).max(), 1e-9)
+                assert abs(ss[1] - so[1]) <= 2 + 1e-3 * so[1]
+
+
+def test_static_linearisation_allocates_nothing(cuda):
+    import torch
+
+    tr, ot, K, gt, keep = _tracker(L.TRACK_RGBD)
+    out = torch.zeros(46, dtype=torch.float64, device="cuda")
+    lv = _level(tr, 0, K)
+    pose = L.pose_from(gt)
+    L.call("yas_gn_linearise_static", C.byref(lv), C.byref(pose), L.TRACK_RGBD, out.data_ptr(), None)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        L.call("yas_gn_linearise_static", C.byref(lv), C.byref(pose), L.TRACK_RGBD, out.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_static_linearisation_rejects_oversized_levels(cuda):

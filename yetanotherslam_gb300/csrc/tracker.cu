@@ -35,6 +35,8 @@
 #include <cfloat>
 #include <cstring>
 
+#include <cuda.h>
+
 #include "gn_solve.cuh"
 #include "yas_track.h"
 
@@ -243,12 +245,14 @@ __device__ void publish_estimate(GNState *st, const double Kd[kMaxLevels][4], in
 // R * K_l^-1 for TransformReferencePoint (ImageProc.cu:86-101), formed in FP32
 // from the FP32 estimate by each CTA (the reference forms it in FP64 and
 // rounds it to FP32; the two differ by an ulp).
+// One rounding per operation, in a fixed order, so that the pixels it sends
+// inside or outside the image are the oracle's.
 __device__ __forceinline__ void make_rkinv(const float *T, const LevelCam &c, float *RK) {
-    const float cxi = c.cx * c.invfx, cyi = c.cy * c.invfy;
+    const float cxi = __fmul_rn(c.cx, c.invfx), cyi = __fmul_rn(c.cy, c.invfy);
     for (int i = 0; i < 3; ++i) {
-        RK[i * 3 + 0] = T[i * 4 + 0] * c.invfx;
-        RK[i * 3 + 1] = T[i * 4 + 1] * c.invfy;
-        RK[i * 3 + 2] = T[i * 4 + 2] - T[i * 4 + 0] * cxi - T[i * 4 + 1] * cyi;
+        RK[i * 3 + 0] = __fmul_rn(T[i * 4 + 0], c.invfx);
+        RK[i * 3 + 1] = __fmul_rn(T[i * 4 + 1], c.invfy);
+        RK[i * 3 + 2] = __fsub_rn(__fsub_rn(T[i * 4 + 2], __fmul_rn(T[i * 4 + 0], cxi)), __fmul_rn(T[i * 4 + 1], cyi));
     }
 }
 
@@ -261,6 +265,85 @@ __device__ __forceinline__ float3 warp_ref_point(const float *RK, const float *T
     p.y = __fadd_rn(__fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(RK[3], fx), __fmul_rn(RK[4], fy)), RK[5]), z), T[7]);
     p.z = __fadd_rn(__fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(RK[6], fx), __fmul_rn(RK[7], fy)), RK[8]), z), T[11]);
     return p;
+}
+
+// The discrete decisions of the tracker (which reference pixels project
+// inside the current image, which model point pairs with which current pixel
+// and passes the ICP gates) and the ICP residual that GetTransform's
+// keep-the-better-estimate test sums are evaluated with one IEEE rounding per
+// operation in a fixed order (no contraction), exactly as the oracle
+// evaluates them, so both sides take the same decisions at the same FP32
+// pose.  A coordinate is tested as a float before it is converted, so a NaN
+// or infinite projection is outside on both sides.
+
+// Photometric projection of a warped reference point (se3StepRGBFunctor's
+// bounds, TrackingUtils.h:73-150): inside when 0 < u < w-1 and 0 < v < h-1.
+__device__ __forceinline__ bool rgb_project(const LevelCam &c, const float3 &p, float &u, float &v) {
+    u = __fadd_rn(__fdiv_rn(__fmul_rn(c.fx, p.x), p.z), c.cx);
+    v = __fadd_rn(__fdiv_rn(__fmul_rn(c.fy, p.y), p.z), c.cy);
+    return u > 0.0f && v > 0.0f && u < (float)(c.w - 1) && v < (float)(c.h - 1);
+}
+
+__device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, float b0, float b1, float b2) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+
+// IcpStepFunctor::ProjectPoint (RGBDTracking.cu:326-358) for model pixel k:
+// the model point and normal moved by T, the nearest current pixel
+// (floor(fx x / z + cx + 0.5)), and the gates |n_c x n_m| < sin 20 deg,
+// |v_m - v_c| <= dist_th, both normals valid.  On success vl, nl, vc and the
+// point-to-plane residual r = n_m . (v_c - v_m) are set.
+__device__ __forceinline__ bool icp_match(const float *T, const LevelCam &c, const float4 *__restrict__ ref_vmap,
+                                          const float4 *__restrict__ ref_nmap, const float4 *__restrict__ cur_vmap,
+                                          const float4 *__restrict__ cur_nmap, int k, float angle_th, float dist_th,
+                                          float3 &vl, float3 &nl, float4 &vc, float &r) {
+    const float4 vm = __ldg(ref_vmap + k);
+    if (!(vm.w >= 0.0f)) return false;
+    vl = make_float3(__fadd_rn(dot3_rn(T[0], T[1], T[2], vm.x, vm.y, vm.z), T[3]),
+                     __fadd_rn(dot3_rn(T[4], T[5], T[6], vm.x, vm.y, vm.z), T[7]),
+                     __fadd_rn(dot3_rn(T[8], T[9], T[10], vm.x, vm.y, vm.z), T[11]));
+    const float invz = __fdiv_rn(1.0f, vl.z);
+    const float fu = floorf(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(c.fx, vl.x), invz), c.cx), 0.5f));
+    const float fv = floorf(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(c.fy, vl.y), invz), c.cy), 0.5f));
+    if (!(fu >= 0.0f && fv >= 0.0f && fu < (float)c.w && fv < (float)c.h)) return false;
+    const int q = (int)fv * c.w + (int)fu;
+    vc = __ldg(cur_vmap + q);
+    if (!(vc.w >= 0.0f)) return false;
+    const float4 nm = __ldg(ref_nmap + k);
+    nl = make_float3(dot3_rn(T[0], T[1], T[2], nm.x, nm.y, nm.z), dot3_rn(T[4], T[5], T[6], nm.x, nm.y, nm.z),
+                     dot3_rn(T[8], T[9], T[10], nm.x, nm.y, nm.z));
+    const float4 nc = __ldg(cur_nmap + q);
+    const float dx = __fsub_rn(vl.x, vc.x), dy = __fsub_rn(vl.y, vc.y), dz = __fsub_rn(vl.z, vc.z);
+    const float dist = __fsqrt_rn(dot3_rn(dx, dy, dz, dx, dy, dz));
+    const float ax = __fsub_rn(__fmul_rn(nc.y, nl.z), __fmul_rn(nc.z, nl.y));
+    const float ay = __fsub_rn(__fmul_rn(nc.z, nl.x), __fmul_rn(nc.x, nl.z));
+    const float az = __fsub_rn(__fmul_rn(nc.x, nl.y), __fmul_rn(nc.y, nl.x));
+    const float angle = __fsqrt_rn(dot3_rn(ax, ay, az, ax, ay, az));
+    if (!(angle < angle_th && dist <= dist_th && nm.w > 0.0f && nc.w > 0.0f)) return false;
+    r = dot3_rn(nl.x, nl.y, nl.z, __fsub_rn(vc.x, vl.x), __fsub_rn(vc.y, vl.y), __fsub_rn(vc.z, vl.z));
+    return true;
+}
+
+// The ICP row [n, v x n | r] of a matched pair, accumulated into the 28
+// products (the r^2 term as the sum of rounded squares, as the oracle sums
+// it) and the count.
+__device__ __forceinline__ void icp_accumulate(const float3 &vl, const float3 &nl, float r, float acc[32]) {
+    float row[6];
+    row[0] = nl.x;
+    row[1] = nl.y;
+    row[2] = nl.z;
+    row[3] = vl.y * nl.z - vl.z * nl.y;
+    row[4] = vl.z * nl.x - vl.x * nl.z;
+    row[5] = vl.x * nl.y - vl.y * nl.x;
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int j = i; j < 6; ++j) acc[q++] += row[i] * row[j];
+        acc[q++] += row[i] * r;
+    }
+    acc[27] = __fadd_rn(acc[27], __fmul_rn(r, r));
+    acc[28] += 1.0f;
 }
 
 __device__ __forceinline__ float bilinear(const float *__restrict__ m, int w, float x, float y) {
@@ -307,11 +390,10 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
             bool ok = false;
             const float zinv = __ldg(a.ref_invd + k);
             if (zinv > 0.0f) {
-                const float z = 1.0f / zinv;
+                const float z = __fdiv_rn(1.0f, zinv);
                 const float3 p = warp_ref_point(sRK, sT, x, y, z);
-                const float u = c.fx * p.x / p.z + c.cx;
-                const float v = c.fy * p.y / p.z + c.cy;
-                if (u > 0.0f && v > 0.0f && u < (float)(c.w - 1) && v < (float)(c.h - 1)) {
+                float u, v;
+                if (rgb_project(c, p, u, v)) {
                     r = bilinear(a.cur_int, c.w, u, v) - __ldg(a.ref_int + k);
                     gx = bilinear(a.cur_gx, c.w, u, v);
                     gy = bilinear(a.cur_gy, c.w, u, v);
@@ -326,46 +408,12 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
             }
         }
         if (do_icp) {
-            const float4 vm = __ldg(a.ref_vmap + k);
-            if (vm.w >= 0.0f) {
-                const float3 vl = make_float3(sT[0] * vm.x + sT[1] * vm.y + sT[2] * vm.z + sT[3],
-                                              sT[4] * vm.x + sT[5] * vm.y + sT[6] * vm.z + sT[7],
-                                              sT[8] * vm.x + sT[9] * vm.y + sT[10] * vm.z + sT[11]);
-                const float invz = 1.0f / vl.z;
-                const int u = (int)floorf(c.fx * vl.x * invz + c.cx + 0.5f);
-                const int v = (int)floorf(c.fy * vl.y * invz + c.cy + 0.5f);
-                if (u >= 0 && v >= 0 && u < c.w && v < c.h) {
-                    const float4 vc = __ldg(a.cur_vmap + v * c.w + u);
-                    if (vc.w >= 0.0f) {
-                        const float4 nm = __ldg(a.ref_nmap + k);
-                        const float3 nl = make_float3(sT[0] * nm.x + sT[1] * nm.y + sT[2] * nm.z,
-                                                      sT[4] * nm.x + sT[5] * nm.y + sT[6] * nm.z,
-                                                      sT[8] * nm.x + sT[9] * nm.y + sT[10] * nm.z);
-                        const float4 nc = __ldg(a.cur_nmap + v * c.w + u);
-                        const float dx = vl.x - vc.x, dy = vl.y - vc.y, dz = vl.z - vc.z;
-                        const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-                        const float cx_ = nc.y * nl.z - nc.z * nl.y, cy_ = nc.z * nl.x - nc.x * nl.z,
-                                    cz_ = nc.x * nl.y - nc.y * nl.x;
-                        const float angle = sqrtf(cx_ * cx_ + cy_ * cy_ + cz_ * cz_);
-                        if (angle < a.angle_th && dist <= a.dist_th && nm.w > 0.0f && nc.w > 0.0f) {
-                            float row[7];
-                            row[0] = nl.x;
-                            row[1] = nl.y;
-                            row[2] = nl.z;
-                            row[3] = vl.y * nl.z - vl.z * nl.y;
-                            row[4] = vl.z * nl.x - vl.x * nl.z;
-                            row[5] = vl.x * nl.y - vl.y * nl.x;
-                            row[6] = nl.x * (vc.x - vl.x) + nl.y * (vc.y - vl.y) + nl.z * (vc.z - vl.z);
-                            int q = 0;
-#pragma unroll
-                            for (int i = 0; i < 7; ++i)
-#pragma unroll
-                                for (int j = i; j < 7; ++j) acc[q++] += row[i] * row[j];
-                            acc[28] += 1.0f;
-                        }
-                    }
-                }
-            }
+            float3 vl, nl;
+            float4 vc;
+            float r;
+            if (icp_match(sT, c, a.ref_vmap, a.ref_nmap, a.cur_vmap, a.cur_nmap, k, a.angle_th, a.dist_th, vl, nl, vc,
+                          r))
+                icp_accumulate(vl, nl, r, acc);
         }
     }
     if (!grid_reduce32(acc, a.partial, a.grow, a.counter, tot, st->plain_sums != 0u)) return;
@@ -548,11 +596,10 @@ __device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float 
     if (do_rgb) {
         const float zinv = __ldg(lv.ref_invd + k);
         if (zinv > 0.0f) {
-            const float z = 1.0f / zinv;
+            const float z = __fdiv_rn(1.0f, zinv);
             p = warp_ref_point(sRK, sT, x, y, z);
-            const float u = c.fx * p.x / p.z + c.cx;
-            const float v = c.fy * p.y / p.z + c.cy;
-            if (u > 0.0f && v > 0.0f && u < (float)(c.w - 1) && v < (float)(c.h - 1)) {
+            float u, v;
+            if (rgb_project(c, p, u, v)) {
                 const float r = bilinear(lv.cur_int, c.w, u, v) - __ldg(lv.ref_int + k);
                 const float gx = bilinear(lv.cur_gx, c.w, u, v);
                 const float gy = bilinear(lv.cur_gy, c.w, u, v);
@@ -567,46 +614,11 @@ __device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float 
         }
     }
     if (do_icp) {
-        const float4 vm = __ldg(lv.ref_vmap + k);
-        if (vm.w >= 0.0f) {
-            const float3 vl = make_float3(sT[0] * vm.x + sT[1] * vm.y + sT[2] * vm.z + sT[3],
-                                          sT[4] * vm.x + sT[5] * vm.y + sT[6] * vm.z + sT[7],
-                                          sT[8] * vm.x + sT[9] * vm.y + sT[10] * vm.z + sT[11]);
-            const float invz = 1.0f / vl.z;
-            const int u = (int)floorf(c.fx * vl.x * invz + c.cx + 0.5f);
-            const int v = (int)floorf(c.fy * vl.y * invz + c.cy + 0.5f);
-            if (u >= 0 && v >= 0 && u < c.w && v < c.h) {
-                const float4 vc = __ldg(lv.cur_vmap + v * c.w + u);
-                if (vc.w >= 0.0f) {
-                    const float4 nm = __ldg(lv.ref_nmap + k);
-                    const float3 nl = make_float3(sT[0] * nm.x + sT[1] * nm.y + sT[2] * nm.z,
-                                                  sT[4] * nm.x + sT[5] * nm.y + sT[6] * nm.z,
-                                                  sT[8] * nm.x + sT[9] * nm.y + sT[10] * nm.z);
-                    const float4 nc = __ldg(lv.cur_nmap + v * c.w + u);
-                    const float dx = vl.x - vc.x, dy = vl.y - vc.y, dz = vl.z - vc.z;
-                    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-                    const float cx_ = nc.y * nl.z - nc.z * nl.y, cy_ = nc.z * nl.x - nc.x * nl.z,
-                                cz_ = nc.x * nl.y - nc.y * nl.x;
-                    const float angle = sqrtf(cx_ * cx_ + cy_ * cy_ + cz_ * cz_);
-                    if (angle < angle_th && dist <= dist_th && nm.w > 0.0f && nc.w > 0.0f) {
-                        float row[7];
-                        row[0] = nl.x;
-                        row[1] = nl.y;
-                        row[2] = nl.z;
-                        row[3] = vl.y * nl.z - vl.z * nl.y;
-                        row[4] = vl.z * nl.x - vl.x * nl.z;
-                        row[5] = vl.x * nl.y - vl.y * nl.x;
-                        row[6] = nl.x * (vc.x - vl.x) + nl.y * (vc.y - vl.y) + nl.z * (vc.z - vl.z);
-                        int q = 0;
-#pragma unroll
-                        for (int i = 0; i < 7; ++i)
-#pragma unroll
-                            for (int j = i; j < 7; ++j) acc[q++] += row[i] * row[j];
-                        acc[28] += 1.0f;
-                    }
-                }
-            }
-        }
+        float3 vl, nl;
+        float4 vc;
+        float r;
+        if (icp_match(sT, c, lv.ref_vmap, lv.ref_nmap, lv.cur_vmap, lv.cur_nmap, k, angle_th, dist_th, vl, nl, vc, r))
+            icp_accumulate(vl, nl, r, acc);
     }
 }
 
@@ -1258,21 +1270,60 @@ struct StaticScratch {
 
 static __device__ __align__(256) StaticScratch g_static_scratch;
 
-// Device address of g_static_scratch per device, resolved once per device.
+// Device address of g_static_scratch, resolved once per device and CUDA
+// context.  The module (and with it the array) is loaded again in a new
+// context, e.g. after cudaDeviceReset, so the cached address is keyed on the
+// context's unique id and resolved again when the current context changes.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+
+struct StaticSlot {
+    unsigned long long ctx_id;
+    StaticScratch *ptr;
+};
 static std::mutex g_static_mutex;
-static StaticScratch *g_static_ptr[64];
+static StaticSlot g_static_slot[64];
+static PfnCtxGetCurrent g_ctx_get_current = nullptr;
+static PfnCtxGetId g_ctx_get_id = nullptr;
+
+// Id of the calling thread's current context (0 when there is none yet).
+// Caller holds g_static_mutex.
+static int current_context_id(unsigned long long *id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1 = cudaDriverEntryPointSymbolNotFound, r2 = r1;
+        YAS_TRY_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &r1));
+        YAS_TRY_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2));
+        if (r1 != cudaDriverEntryPointSuccess || r2 != cudaDriverEntryPointSuccess || !p || !q) return YAS_ERR_STATE;
+        g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(p);
+        g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(q);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return YAS_ERR_STATE;
+    *id = 0;
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return YAS_ERR_STATE;
+    return YAS_OK;
+}
 
 static int static_scratch(StaticScratch **out) {
     int dev = 0;
     YAS_TRY_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return YAS_ERR_STATE;
     std::lock_guard<std::mutex> lk(g_static_mutex);
-    if (!g_static_ptr[dev]) {
+    unsigned long long id = 0;
+    YAS_TRY(current_context_id(&id));
+    StaticSlot &slot = g_static_slot[dev];
+    if (!slot.ptr || id == 0 || slot.ctx_id != id) {
+        // cudaGetSymbolAddress also makes the device's primary context current
+        // when no context is yet, so the id is read again afterwards
         void *p = nullptr;
         YAS_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-        g_static_ptr[dev] = static_cast<StaticScratch *>(p);
+        YAS_TRY(current_context_id(&id));
+        if (id == 0) return YAS_ERR_STATE;
+        slot.ptr = static_cast<StaticScratch *>(p);
+        slot.ctx_id = id;
     }
-    *out = g_static_ptr[dev];
+    *out = slot.ptr;
     return YAS_OK;
 }
 
@@ -1297,6 +1348,13 @@ extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas
         return YAS_ERR_BAD_ARG;
     if ((mode & YAS_TRACK_ICP) && (!lv->ref_vmap || !lv->ref_nmap || !lv->cur_vmap || !lv->cur_nmap))
         return YAS_ERR_BAD_ARG;
+    LevelCam cam;
+    memset(&cam, 0, sizeof(cam));
+    cam.w = lv->width;
+    cam.h = lv->height;
+    // the pass grid must fit the static partial-sum rows and tickets
+    const int g = pass_grid(cam);
+    if (g > kStaticMaxCtas) return YAS_ERR_CAPACITY;
     StaticScratch *sc = nullptr;
     YAS_TRY(static_scratch(&sc));
     cudaStream_t s = (cudaStream_t)stream;
@@ -1337,7 +1395,6 @@ extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas
     a.Kd[0][2] = lv->cx;
     a.Kd[0][3] = lv->cy;
     gn_init_kernel<<<1, 32, 0, s>>>(a.st, pose_from(*T), 1, a);
-    const int g = pass_grid(a.c);
     a.partial = sc->partialA;
     a.grow = sc->growA;
     a.counter = sc->counters;
