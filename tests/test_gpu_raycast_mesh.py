@@ -5,10 +5,13 @@ identical TSDF ("for a given TSDF").  Reference behaviour:
 RGBDFusion/src/RayTraceEngine.cu:58-450, RGBDFusion/src/MeshEngine.cu:43-339.
 Bars:
   * z-range tile maps: bit-exact (FP32 canonical projection);
-  * raycast: hit/miss agreement on >= 99.8 % of pixels; on pixels both hit,
-    |dz| <= 0.1 mm for 99.9 % of them and > 1 mm on at most 0.01 % of them
-    (the march is FP32 on the GPU and FP64 in the oracle, so a ray grazing a
-    silhouette may step onto another surface on one side only);
+  * raycast at 640x480: hit/miss differs on at most 20 pixels (measured 1-3
+    of 307 200); on pixels both hit, |dz| <= 0.01 mm for 99.9 % of them
+    (measured 1.9e-6 m) and > 1 mm on at most 20 pixels (measured 3-5).  The
+    march is FP32 on the GPU and FP64 in the oracle, and the GPU jumps the
+    samples inside unallocated blocks and before the pixel's near bound in one
+    move where the oracle steps voxel by voxel, so a ray grazing a silhouette
+    may step onto another surface on one side only;
   * marching cubes: multiset of (cube, case index) bit-exact; vertex
     positions within 1e-5 m; normals of triangles larger than 1e-7 m^2
     within 1e-3.
@@ -54,12 +57,14 @@ def test_raycast_matches_oracle(cuda, fmt):
     assert np.array_equal(gzn, zn) and np.array_equal(gzf, zf), "z-range tiles differ"
     hg, ho = vg[..., 3] > 0, vo[..., 3] > 0
     agree = (hg == ho).mean()
-    assert hg.mean() > 0.5
-    assert agree >= 0.998, f"hit agreement {agree:.5f}"
     both = hg & ho
     dz = np.abs(vg[..., 2][both] - vo[..., 2][both])
-    assert np.quantile(dz, 0.999) <= 1e-4, f"p99.9 |dz| {np.quantile(dz, 0.999):.3g}"
-    assert (dz > 1e-3).mean() <= 1e-4, f"{(dz > 1e-3).sum()} pixels off by > 1 mm"
+    print(f"raycast fmt {fmt}: hit/miss flips {int((hg != ho).sum())} of {hg.size}, |dz| p99.9 "
+          f"{np.quantile(dz, 0.999):.3g} m, > 1 mm {int((dz > 1e-3).sum())}")
+    assert hg.mean() > 0.5
+    assert (hg != ho).sum() <= 20, f"hit agreement {agree:.6f}"
+    assert np.quantile(dz, 0.999) <= 1e-5, f"p99.9 |dz| {np.quantile(dz, 0.999):.3g}"
+    assert (dz > 1e-3).sum() <= 20, f"{(dz > 1e-3).sum()} pixels off by > 1 mm"
     # VMapToDepth (GetRayTracingResultDepth)
     d = rc.GetDepth()
     assert np.array_equal(d, np.where(hg, vg[..., 2], 0).astype(np.float32))

@@ -284,9 +284,10 @@ __device__ __forceinline__ bool ray_step(VoxelReader<FMT> &rd, float rstep, RayS
         // Unallocated block: every sample until the ray leaves it reads
         // "unobserved" and advances one voxel, so those samples are skipped in
         // one move.  k = steps to the first sample outside the block on the
-        // earliest exit axis; two are kept as margin against rounding, so the
-        // samples evaluated next are the last ones inside the block (evaluated
-        // normally).
+        // earliest exit axis.  When sample k - 1 (computed as the jump computes
+        // it) is still in the block and sample k is not, the ray jumps straight
+        // to sample k; otherwise (k rounded the wrong way) it keeps two samples
+        // as margin and evaluates the last ones inside the block normally.
         R.skipped = rd.ckey;
         const float bx0 = floorf(floorf(R.r.x) * 0.125f) * 8.0f;
         const float by0 = floorf(floorf(R.r.y) * 0.125f) * 8.0f;
@@ -297,7 +298,19 @@ __device__ __forceinline__ bool ray_step(VoxelReader<FMT> &rd, float rstep, RayS
                                         : (R.dir.y < 0.0f ? floorf((by0 - R.r.y) * R.idir.y) + 1.0f : 1e30f);
         const float kz = R.dir.z > 0.0f ? ceilf((bz0 + 8.0f - R.r.z) * R.idir.z)
                                         : (R.dir.z < 0.0f ? floorf((bz0 - R.r.z) * R.idir.z) + 1.0f : 1e30f);
-        const float n = fminf(fminf(fminf(kx, ky), kz) - 2.0f, ceilf(R.dist_e - R.dist_s));
+        const float k = fminf(fminf(kx, ky), kz);
+        float n = k - 2.0f;
+        if (k >= 1.0f && k < 1e29f) {
+            const float a = k - 1.0f;
+            const float3 pin = make_float3(R.r.x + a * R.dir.x, R.r.y + a * R.dir.y, R.r.z + a * R.dir.z);
+            const float3 pout = make_float3(R.r.x + k * R.dir.x, R.r.y + k * R.dir.y, R.r.z + k * R.dir.z);
+            const unsigned long long kin =
+                pack_key((int)floorf(pin.x) >> 3, (int)floorf(pin.y) >> 3, (int)floorf(pin.z) >> 3);
+            const unsigned long long kout =
+                pack_key((int)floorf(pout.x) >> 3, (int)floorf(pout.y) >> 3, (int)floorf(pout.z) >> 3);
+            if (kin == rd.ckey && kout != rd.ckey) n = k;
+        }
+        n = fminf(n, ceilf(R.dist_e - R.dist_s));
         if (n >= 1.0f) {
             R.r.x += n * R.dir.x;
             R.r.y += n * R.dir.y;
