@@ -268,6 +268,13 @@ YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated);
  * when the limit works).  The tracker stays usable; its next GetTransform
  * starts from a reset state.  Takes about one second. */
 YAS_API int yas_tracker_check_wait_limit(yas_tracker *tr, int *out_status);
+/* Checks the FP64 division the device solve uses for its pivots (no
+ * counterpart in the reference: the reference divides on the host in Eigen).
+ * out[i] = a[i] / x[i] computed on the device as the solve computes it:
+ * Newton-Raphson refinement (one step) of an FP32 reciprocal seed for
+ * 1e-30 < |x| < 1e30, IEEE division outside that range.  Host arrays of n
+ * doubles, 0 < n <= 1 << 20; waits for the result. */
+YAS_API int yas_check_div_seeded(const double *a, const double *x, double *out, int n);
 /* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);
 YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);

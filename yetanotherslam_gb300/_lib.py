@@ -122,6 +122,7 @@ _SIGS = {
     "yas_copy_to_host": [_P, _I, _P, _I, _I, _I],
     "yas_tracker_set_reduction": [_P, _I],
     "yas_tracker_check_wait_limit": [_P, _PI],
+    "yas_check_div_seeded": [_P, _P, _P, C.c_int],
     "yas_pyr_down_depth": [_P, _I, _I, _I, _P, _I, _I, _I, _P],
     "yas_depth_to_inv_depth": [_P, _I, _I, _I, _P, _I, _P],
     "yas_compute_vertex_map": [_P, _I, _I, _I, _P, _I, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _P],

@@ -1,9 +1,14 @@
 """Batched keyframe submaps: ``yas_batch_*`` of ``include/yas.h``.
 
 Many sessions (submaps of any resolution and voxel size) step together; one
-step is one CUDA graph launch holding every active session's frame, with a
-single persistent Gauss-Newton launch for all of them.  ``autotune`` picks the
-launch shapes on scratch copies of the sessions.
+step is one CUDA graph launch holding every active session's frame.  By
+default (``gn_per_session = 1``) each session's whole Gauss-Newton schedule
+is its own cooperative launch in that session's branch of the graph, so a
+session's pose update and fusion start as soon as its own GN ends; with
+``gn_per_session = 0`` one persistent cooperative launch runs every
+session's schedule.  Both give the same results.  ``autotune`` picks the
+launch shapes (and between these two modes) on scratch copies of the
+sessions.
 """
 from __future__ import annotations
 

@@ -83,9 +83,12 @@ __device__ __forceinline__ double rcp_seed(double x) {
     return __hiloint2double((int)hi2, (int)((rb & 0x7fffffu) << 29));
 }
 
-// a / x: seed r, e = 1 - x r, a r (1 + e) (relative error ~2^-44, far below
-// the ~1e-7 precision of the FP32-accumulated system it is applied to);
-// outside the seed range an IEEE division.
+// a / x by one Newton-Raphson refinement of an FP32 reciprocal seed: with the
+// seed r = (1 - d) / x (|d| < 2^-22), e = 1 - x r = d and a r (1 + e) =
+// (a / x)(1 - d^2), a relative error below 2^-44 plus the FP64 roundings
+// (far below the ~1e-7 precision of the FP32-accumulated system it is applied
+// to); outside the seed range an IEEE division.  yas_check_div_seeded
+// evaluates it for the tests.
 __device__ __forceinline__ double div_seeded(double a, double x) {
     if (!seed_range(x)) return a / x;
     const double r = rcp_seed(x);

@@ -1409,3 +1409,28 @@ extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas
     YAS_TRY_CUDA(cudaGetLastError());
     return YAS_OK;
 }
+
+// ---------------------------------------------------------------- self-check of the seeded division
+namespace yas {
+__global__ void div_seeded_kernel(const double *a, const double *x, double *out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = div_seeded(a[i], x[i]);
+}
+}  // namespace yas
+
+extern "C" YAS_API int yas_check_div_seeded(const double *a, const double *x, double *out, int n) {
+    using namespace yas;
+    if (!a || !x || !out || n <= 0 || n > (1 << 20)) return YAS_ERR_BAD_ARG;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    double *d = nullptr;
+    YAS_TRY_CUDA(cudaMalloc(&d, 3 * bytes));
+    cudaError_t e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, x, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        div_seeded_kernel<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? YAS_OK : YAS_ERR_CUDA;
+}
