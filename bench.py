@@ -18,7 +18,15 @@ region (wall clock around the synchronous process call).
 
 ``--impl reference`` times the CPU restatement of the reference's path
 (the oracle built in FP32 with OpenMP on every host core) on the same
-workload, on a bounded number of frames.
+workload and the same number of warm-up and timed frames.
+
+Also on the line: ``cpu_baseline`` (the same restatement timed on 8 frames)
+and ``precision`` (the benchmarked form against the oracle's FP64 build on
+the first 30 frames), both from the CPU-baseline leg; ``served`` (32
+sessions, Poisson arrivals), ``batched`` (16 submaps) and ``large`` (the
+2000-frame 1280x720 / 4 mm loop with de-/re-integration and full-map
+marching cubes), each skippable with ``--served 0`` / ``--batched 0`` /
+``--large 0``.
 """
 from __future__ import annotations
 
@@ -38,12 +46,16 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "frames/sec tracking+fusion @640x480/5mm; p50/p99 frame latency at 32 sessions"
+# The workload both arms run (their JSON lines carry this same `config`); what
+# differs between them (the TSDF storage, the arithmetic) is in top-level keys.
 WORKLOAD = {
     "workload": "single-session tracking+fusion, 640x480, 5 mm voxels, seeded synthetic RGB-D sequence",
     "width": 640, "height": 480, "voxel_m": 0.005, "trunc_m": 0.015, "hash_slots": 1 << 21,
-    "max_blocks": 1 << 18, "tsdf": "fp16 + u8 weight + fp16 rounding residual (4 B)", "pyramid_levels": 3, "gn_iterations": [10, 5, 3],
+    "max_blocks": 1 << 18, "pyramid_levels": 3, "gn_iterations": [10, 5, 3],
     "mode": "rgb+icp", "scene_seed": 1,
+    "l2": "GPU arm: flushed between steps (a 256 MB write outside the timed events)",
 }
+GPU_STORAGE = "fp16 sdf + u8 weight + fp16 rounding residual (4 B per voxel)"
 
 
 def rank_max(x: float) -> float:
@@ -283,7 +295,7 @@ def run_gpu(args):
     s2.close()
 
     # ---------------- CPU baseline: the oracle (FP32, OpenMP) on a bounded sample
-    cpu = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else None
+    cpu, precision = cpu_baseline(frames, K, args.cpu_frames) if rank == 0 else (None, None)
     served = run_served(seeds["served"], args.served_gn) if args.served else None
     batched = run_batched(seeds["batched"]) if args.batched else None
     large = run_large(args.large_frames) if args.large else None
@@ -302,12 +314,13 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "fp32 compute, fp16 TSDF storage, fp64 solve",
         "data": "synthetic (seeded analytic RGB-D scene; no dataset)",
-        "config": dict(WORKLOAD, l2="flushed between steps (256 MB write outside the timed events)",
-                       parallelism="replicas" if world > 1 else "single session",
-                       p50_ms=round(lat[len(lat) // 2], 4), p99_ms=round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
-                       frame_status_nonzero=int(sum(1 for x in statuses if x != 0)),
-                       stage_ms_per_frame={stage_name(k): round(v, 4) for k, v in sorted(per_frame.items())},
-                       visible_blocks=nvis),
+        "config": dict(WORKLOAD),
+        "storage": GPU_STORAGE,
+        "parallelism": "replicas" if world > 1 else "single session",
+        "frame": {"p50_ms": round(lat[len(lat) // 2], 4), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
+                  "frame_status_nonzero": int(sum(1 for x in statuses if x != 0)),
+                  "stage_ms_per_frame": {stage_name(k): round(v, 4) for k, v in sorted(per_frame.items())},
+                  "visible_blocks": nvis},
         "e2e": {"value": round(whole_job_rate(world, args.steps, e2e_s), 2), "unit": "frames/s",
                 "h2d_bytes_per_step": W * H * 3 + W * H * 2, "d2h_bytes_per_step": 256},
         "gpu_launches": kernels * args.steps,
@@ -316,6 +329,7 @@ def run_gpu(args):
                      "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": round(per_launch[dom], 5),
                      "traffic": traffic},
         "cpu_baseline": cpu,
+        "precision": precision,
         "served": served,
         "batched": batched,
         "large": large,
@@ -668,7 +682,11 @@ def pose_error_np(A, B):
     return float(np.linalg.norm(E[:3, 3])), float(np.arccos(c))
 
 
-def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
+def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0, check_frames: int = 30):
+    """The CPU-baseline leg: the oracle's FP32 build (OpenMP on every host core)
+    timed on a bounded sample of the workload; and the oracle's FP64 build as
+    the checker of the benchmarked form on a prefix of the same sequence.
+    Returns (cpu_baseline, precision)."""
     import oracle
 
     W, H = WORKLOAD["width"], WORKLOAD["height"]
@@ -682,8 +700,78 @@ def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return {"value": round(n / dt, 3), "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{n} tracked frames (after the initialising frame) of the same 640x480 5 mm sequence"}
+    cpu = {"value": round(n / dt, 3), "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
+           "sample": f"{n} tracked frames (after the initialising frame) of the same 640x480 5 mm sequence"}
+    return cpu, precision_check(frames[:check_frames], K)
+
+
+def precision_check(frames, K):
+    """The benchmarked form (FP16 TSDF words, compensated sums, FP64 solve)
+    against the FP64 oracle on a prefix of the benchmark's sequence:
+    - tracking, closed loop: the session's pose and each frame's motion
+      estimate against the oracle session's (metres / radians);
+    - mapping: a map with the same storage fused with the oracle's poses and
+      the same depth against the oracle's FP64 map: TSDF error (normalised by
+      the truncation) on voxels both observe, and the fraction of observed
+      voxels whose weights are equal."""
+    import oracle
+    from yetanotherslam_gb300 import rgbdfusion as rf
+
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    vs, tr = WORKLOAD["voxel_m"], WORKLOAD["trunc_m"]
+    t0 = time.perf_counter()
+    sess = rf.Session(W, H, K, hash_slots=WORKLOAD["hash_slots"], max_blocks=WORKLOAD["max_blocks"], voxel_size=vs,
+                      trunc_dist=tr, voxel_format=rf.VOXEL_F16, num_levels=3, iterations=GN_ITERS)
+    orc = oracle.Session(W, H, K, vs, tr, levels=3, iters=GN_ITERS, kind="f64")
+    m = rf.MapStruct(K)
+    m.create_config(WORKLOAD["hash_slots"], WORKLOAD["max_blocks"], vs, tr, rf.VOXEL_F16)
+    om = oracle.Map(vs, tr)
+    pose_t, pose_r, step_t, step_r = [], [], [], []
+    prev_g = prev_o = None
+    for f in frames:
+        st_o, To = orc.frame(f.rgb, f.depth)
+        st_g, Tg = sess.process(f.rgb, f.depth)
+        if st_o != 0 or st_g != 0:
+            return {"error": f"frame status gpu={st_g} oracle={st_o}"}
+        e = pose_error_np(To, Tg)
+        pose_t.append(e[0])
+        pose_r.append(e[1])
+        if prev_o is not None:
+            e = pose_error_np(np.linalg.inv(prev_o) @ To, np.linalg.inv(prev_g) @ Tg)
+            step_t.append(e[0])
+            step_r.append(e[1])
+        prev_g, prev_o = Tg, To
+        dm = f.depth.astype(np.float32) * np.float32(0.001)
+        m.Fuse(dm, To)
+        om.fuse(dm, K, To)
+    sess.close()
+    cg, sg, wg = m.export()
+    co, so, wo = om.export()
+
+    def keys(c):
+        c = c.astype(np.int64) + (1 << 20)
+        return (c[:, 0] << 42) | (c[:, 1] << 21) | c[:, 2]
+
+    kg, ko = keys(cg), keys(co)
+    common, ig, io = np.intersect1d(kg, ko, return_indices=True)
+    sg, wg, so, wo = sg[ig], wg[ig], so[io], wo[io]
+    both = (wg > 0) & (wo > 0)
+    same = both & (wg == wo)
+    d = np.abs(sg[same].astype(np.float64) - so[same])
+
+    def st(x):
+        x = np.asarray(x, np.float64)
+        return {"max": float(x.max()), "p99": float(np.percentile(x, 99)), "p50": float(np.median(x))}
+
+    return {"against": "the oracle's FP64 build (checker), same frames",
+            "form": GPU_STORAGE + ", compensated FP32 sums, FP64 solve",
+            "frames": len(frames),
+            "pose_m": st(pose_t), "pose_rad": st(pose_r),
+            "frame_motion_m": st(step_t), "frame_motion_rad": st(step_r),
+            "tsdf_x_trunc": st(d) if d.size else None,
+            "weights_equal_frac": round(float(same.sum() / max(int(both.sum()), 1)), 6),
+            "blocks": {"gpu": int(kg.size), "oracle": int(ko.size), "common": int(common.size)},
+            "seconds": round(time.perf_counter() - t0, 1)}
 
 
 def run_reference(args):
@@ -695,8 +783,8 @@ def run_reference(args):
 
     W, H = WORKLOAD["width"], WORKLOAD["height"]
     K = synth.intrinsics(W, H)
-    warm = max(3, min(args.warmup, 5))  # at least 3 untimed frames, as the GPU arm
-    steps = min(args.steps, args.cpu_frames)
+    warm = max(3, args.warmup)  # the GPU arm's untimed frames
+    steps = args.steps  # the GPU arm's timed frames
     frames = make_frames(1 + warm + steps, W, H, WORKLOAD["scene_seed"])
     import oracle as orc
 
@@ -709,7 +797,7 @@ def run_reference(args):
     for f in frames[1 + warm:]:
         o.frame(f.rgb, f.depth)
         n += 1
-        if time.perf_counter() - t0 > 150.0:
+        if time.perf_counter() - t0 > 600.0:  # a bound far above 100 frames' 20 s
             break
     dt = time.perf_counter() - t0
     v = round(n / dt, 3)
@@ -717,8 +805,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 0,
         "steps": n, "warmup": warm, "ms_per_step": round(1e3 * dt / max(n, 1), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": dict(WORKLOAD, note="CPU restatement of the reference's dense path (the reference needs OpenCV "
-                                      "CUDA, Eigen, Sophus and does not build here); FP32, OpenMP"),
+        "config": dict(WORKLOAD),
+        "storage": "fp32 sdf + fp32 weight (the restatement's FP32 build)",
+        "note": "CPU restatement of the reference's dense path (the reference needs OpenCV CUDA, Eigen and Sophus "
+                "and does not build here); FP32 arithmetic, OpenMP over every host core",
         "cpu_baseline": {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{n} tracked frames of the 640x480 5 mm sequence"},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -739,7 +829,7 @@ def main():
     ap.add_argument("--served-ppc", type=int, default=0,
                     help="served sessions, GN per session: level-0 pixels per CTA of a session's share (0: default)")
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
-    ap.add_argument("--large", type=int, default=0, help="1: also run the 2000-frame 1280x720 large map (C5)")
+    ap.add_argument("--large", type=int, default=1, help="1: also run the 2000-frame 1280x720 large map (C5)")
     ap.add_argument("--large-frames", type=int, default=2000)
     ap.add_argument("--leg", choices=["served", "batched", "batched-pass", "large"], default=None,
                     help="run only this workload and print its result (for profiling one leg)")

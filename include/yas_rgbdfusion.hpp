@@ -18,7 +18,10 @@
  *                        optionally owning its memory (shared).
  * Define YAS_SHIM_SOPHUS before including to use Sophus::SE3d (and Eigen's
  * matrices) directly, and YAS_SHIM_OPENCV to add cv::Mat / cv::cuda::GpuMat
- * overloads of every image argument.
+ * overloads of every image argument and to return GpuMats from
+ * MapStruct::GetRayTracingResult / GetRayTracingResultDepth, as the reference
+ * does.  The OpenCV branch expects the caller on the legacy default stream
+ * (engines created with a NULL stream), as FullSystem is.
  *
  * Errors.  The reference exits the process on a CUDA error (SafeCall).  Here
  * every failing call throws yas::shim::Error, which carries the yas_status.
@@ -415,8 +418,27 @@ public:
     void RayTrace(const SE3d &Tcm) {
         if (mpRayTraceEngine) mpRayTraceEngine->RayTrace(this, Tcm);
     }
+#ifdef YAS_SHIM_OPENCV
+    /* GetRayTracingResult() (VoxelMap.cu:976-979): a CV_32FC4 GpuMat header
+     * aliasing the engine's vertex map; the next raycast overwrites it. */
+    cv::cuda::GpuMat GetRayTracingResult() {
+        if (!mpRayTraceEngine) return cv::cuda::GpuMat();
+        const Image v = mpRayTraceEngine->GetVMap();
+        return cv::cuda::GpuMat(v.rows, v.cols, CV_32FC4, v.data, v.step);
+    }
+    /* GetRayTracingResultDepth() (VoxelMap.cu:981-987): VMapToDepth of the
+     * last raycast into a new CV_32FC1 device image. */
+    cv::cuda::GpuMat GetRayTracingResultDepth() {
+        if (!mpRayTraceEngine) return cv::cuda::GpuMat();
+        const Image v = mpRayTraceEngine->GetVMap();
+        cv::cuda::GpuMat d(v.rows, v.cols, CV_32FC1);
+        check(yas_raycaster_depth(mpRayTraceEngine->handle(), d.ptr<float>(), (int)d.step, 1));
+        return d;
+    }
+#else
     Image GetRayTracingResult() { return mpRayTraceEngine ? mpRayTraceEngine->GetVMap() : Image(); }
     Image GetRayTracingResultDepth() { return mpRayTraceEngine ? mpRayTraceEngine->GetDepth() : Image(); }
+#endif
 
     yas_map *handle() const { return handle_; }
     yas_map *require() const {

@@ -183,3 +183,110 @@ def _num_rendering(L, rt) -> int:
     out = C.c_uint()
     L.call("yas_raycaster_num_rendering_blocks", rt.handle, C.byref(out))
     return out.value
+
+
+# --- FullSystem's own types: the YAS_SHIM_SOPHUS / YAS_SHIM_OPENCV branches --
+FS_DRIVER = ROOT / "tests" / "cpp" / "shim_fullsystem.cpp"
+STANDIN = ROOT / "tests" / "cpp" / "standin"
+
+
+def _cuda_root() -> Path:
+    import shutil
+
+    nvcc = shutil.which("nvcc")
+    return Path(nvcc).resolve().parent.parent if nvcc else Path("/usr/local/cuda")
+
+
+def _compile_fullsystem(out: Path) -> Path:
+    """The FullSystem-typed driver against the header with both reference-type
+    branches on, and the stand-in Eigen / Sophus / OpenCV headers (the
+    stand-in GpuMat links the CUDA runtime for its copies, as OpenCV does)."""
+    from yetanotherslam_gb300 import build
+
+    lib_dir = build.LIB.parent
+    cuda = _cuda_root()
+    cudalib = cuda / "lib64" if (cuda / "lib64").exists() else cuda / "lib"
+    cmd = ["g++", *FLAGS, "-DYAS_SHIM_SOPHUS", "-DYAS_SHIM_OPENCV", f"-I{STANDIN}", f"-I{ROOT / 'include'}",
+           f"-I{cuda / 'include'}", str(FS_DRIVER), f"-L{lib_dir}", "-lyas_gb300", f"-L{cudalib}", "-lcudart",
+           f"-Wl,-rpath,{lib_dir}", f"-Wl,-rpath,{cudalib}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_fullsystem_typed_shim_compiles_and_links(native, tmp_path):
+    """Tracking.cpp's calls with Sophus::SE3d, Eigen::Matrix3f/3d, cv::Mat and
+    cv::cuda::GpuMat (VoxelMap.h:32-144, RGBDTracking.h:9-107) compile
+    warning-free against the header's YAS_SHIM_SOPHUS and YAS_SHIM_OPENCV
+    branches and link against libyas_gb300."""
+    _compile_fullsystem(tmp_path / "shim_fullsystem")
+
+
+@pytest.mark.gpu
+def test_fullsystem_typed_shim_tracks_like_python_classes(cuda, tmp_path):
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import synth
+
+    W, H, n = 320, 240, 10
+    fx, fy, cx, cy = synth.intrinsics(W, H)
+    seq = sequence(3, n, W, H)
+    grays = [synth.gray_of(rgb) for rgb, _, _, _ in seq]
+    frames = tmp_path / "frames.bin"
+    with open(frames, "wb") as f:
+        f.write(np.array([W, H, n], np.int32).tobytes())
+        f.write(np.array([fx, fy, cx, cy], np.float32).tobytes())
+        for g, (_, _, dm, _) in zip(grays, seq):
+            f.write(np.ascontiguousarray(g, np.uint8).tobytes())
+            f.write(np.ascontiguousarray(dm, np.float32).tobytes())
+    exe = _compile_fullsystem(tmp_path / "shim_fullsystem")
+    out = tmp_path / "out.txt"
+    r = subprocess.run([str(exe), str(frames), str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, (r.stdout, r.stderr, out.read_text() if out.exists() else "")
+    got = _parse(out)
+
+    # the same calls through the Python mirror (FullSystem's 5-level tracker,
+    # create(5000, 4000, 4500, 0.01, 0.03))
+    K3 = np.array([[fx, 0, cx], [0, fy, cy], [0, 0, 1]], np.float64)
+    K4 = np.float32([fx, fy, cx, cy])
+    tr = rf.RGBDTracking(W, H, K3, True, True)
+    rt = rf.RayTraceEngine(W, H, K4)
+    me = rf.MeshEngine(1 << 21)
+    ms = rf.MapStruct(K4)
+    ms.create(5000, 4000, 4500, 0.01, 0.03)
+    Tcp = np.eye(4)
+    poses = []
+    for i, (g, (_, _, dm, _)) in enumerate(zip(grays, seq)):
+        st = 0
+        if i == 0:
+            tr.SetReferenceImage(g)
+            tr.SetReferenceDepth(dm)
+            ms.Fuse(dm, Tcp)
+        else:
+            rt.RayTrace(ms, Tcp)
+            tr.SetReferenceModel(rt.GetVMap())
+            tr.SetTrackingImage(g)
+            tr.SetTrackingDepth(dm)
+            DT = tr.GetTransform(np.eye(4), True)
+            if np.sqrt(DT[0, 3] ** 2 + DT[1, 3] ** 2 + DT[2, 3] ** 2) > 0.1:
+                st = 7
+            else:
+                Tcp = _mul(Tcp, _inv(DT))
+                ms.Fuse(dm, Tcp)
+        poses.append((st, Tcp.copy()))
+
+    assert len(got["pose"]) == n
+    gt = rel_poses(seq)
+    for i, ((st_c, Tc), (st_p, Tp)) in enumerate(zip(got["pose"], poses)):
+        assert st_c == st_p == 0, i
+        assert np.abs(Tc - Tp[:3, :4].reshape(-1)).max() <= 1e-12, f"frame {i}"
+        et, er = pose_error(gt[i], Tp)
+        assert et < 0.05 and er < 0.02
+    assert got["good"] == ["1"]
+    depth = rt.GetDepth()
+    pos = depth[depth > 0]
+    assert float(got["keyframe_depth"][0]) == _seq_sum(pos) and int(got["keyframe_depth"][1]) == pos.size > 0
+    pts, _, _, _ = me.Meshify(ms)
+    assert int(got["mesh"][0]) == pts.size > 0 and got["mesh"][1] == "1"
+    sw = got["switch"]
+    assert sw[:2] == ["0", "1"]
+    assert np.allclose([float(x) for x in sw[2:]], Tcp[:3, 3], atol=1e-12)
