@@ -5,11 +5,16 @@
 // Semantics:
 //   H = H_rgb + 100 H_icp, b = b_rgb + 10 b_icp (RGBDTracking.cu:543-544);
 //   error = sqrt(residualSum) / (numResidual + 6), in FP32 as the reference;
-//   update = LDLT(H).solve(b) in FP64: LDL^T with diagonal pivoting (largest
-//   remaining |diagonal|, first on ties, a NaN never chosen), pseudo-inverse
-//   of D (|d| <= 1/DBL_MAX -> 0), identity transpositions and no factorisation
-//   if the first pivot is zero, L columns of later zero pivots left undivided
-//   (Eigen 3's LDLT);
+//   update = LDLT(H).solve(b) in FP64: LDL^T with symmetric diagonal
+//   pivoting, pseudo-inverse of D (|d| <= 1/DBL_MAX -> 0), identity
+//   transpositions and no factorisation if the largest diagonal is zero (or
+//   the first is NaN), L columns of later zero pivots left undivided (Eigen 3's
+//   LDLT).  The pivot order is fixed once from the initial |diagonal| (largest
+//   first, first on ties, NaN last) where Eigen re-selects the largest
+//   remaining diagonal at every step: for the positive semi-definite H of a
+//   Gauss-Newton step both orders give the same solution up to rounding
+//   (1e-15 relative measured), and the fixed order saves a pivot search and a
+//   row swap per step on the solve's serial chain;
 //   NaN in update(0): the iteration fails and the result is the identity;
 //   estimate = exp(update) * estimate (SE(3) exponential, FP64);
 //   the kept estimate is the one after an update whose error (measured before
@@ -19,10 +24,13 @@
 // or without dependencies, so the cost of the solve is its count of FP64 warp
 // instructions.  The layout minimises that count: lane 0..20 holds one element
 // (i, j), j <= i, of the lower triangle of H, lanes 21..26 hold b, so one
-// elimination step is four FP64 instructions for the whole trailing matrix
+// elimination step is five FP64 instructions for the whole trailing matrix
 // and b; pivot tests, NaN tests and reciprocal seeds are integer bit
 // operations; the SE(3) exponential computes its three series on three lanes
-// and one entry of [R | t] per lane.
+// and one entry of [R | t] per lane.  An elimination step divides through the
+// pivot's reciprocal (an FP32 seed refined by one Newton-Raphson step), so the
+// products a_ik a_jk of the trailing update are formed while the reciprocal is
+// refined.
 #pragma once
 
 #include <cfloat>
@@ -34,12 +42,6 @@ namespace yas {
 // Packed index k of the 28 products of [J | r]: rows i, columns j >= i
 // (RankUpdateHessian<6,7>, TrackingUtils.h:45-58).
 __device__ __forceinline__ int pack_index(int r, int c) { return 7 * r - (r * (r - 1)) / 2 + c - r; }
-
-// Taylor coefficients (in th^2) of sin(th)/th, (1-cos th)/th^2, (th-sin th)/th^3.
-__constant__ double c_exp_poly[3][5] = {
-    {1.0, -1.0 / 6.0, 1.0 / 120.0, -1.0 / 5040.0, 1.0 / 362880.0},
-    {0.5, -1.0 / 24.0, 1.0 / 720.0, -1.0 / 40320.0, 1.0 / 3628800.0},
-    {1.0 / 6.0, -1.0 / 120.0, 1.0 / 5040.0, -1.0 / 362880.0, 1.0 / 39916800.0}};
 
 // Inputs, state and outputs of the solve, in the shared memory of the CTA
 // that runs it.
@@ -96,6 +98,19 @@ __device__ __forceinline__ double div_seeded(double a, double x) {
     return fma(q0, fma(-x, r, 1.0), q0);
 }
 
+// (float)x, rounded to nearest even, by integer operations for a value in the
+// normal FP32 range (the conversion instruction otherwise; same result).
+__device__ __forceinline__ float to_float_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e < 897u || e > 1150u) return (float)x;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    unsigned f = (unsigned)(b >> 63) << 31 | (e - 896u) << 23 | (unsigned)(m >> 29);
+    const unsigned rem = (unsigned)(m & 0x1fffffffull);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ++f;  // a carry rounds into the exponent
+    return __uint_as_float(f);
+}
+
 __device__ __forceinline__ double combine_sys(int mode, double a, double b, double wa) {
     return mode == YAS_TRACK_RGBD ? fma(wa, a, b) : (mode == YAS_TRACK_RGB ? b : a);
 }
@@ -113,7 +128,7 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
     // ---- this lane's element: (ei, ej) of the lower triangle, or b[ei] (ej = 6)
     int ei = 0, ej = 7;
     if (lane < 21) {
-        while (tri_lane(ei + 1, 0) <= lane) ++ei;
+        ei = (lane >= 1) + (lane >= 3) + (lane >= 6) + (lane >= 10) + (lane >= 15);
         ej = lane - tri_lane(ei, 0);
     } else if (lane < 27) {
         ei = lane - 21;
@@ -129,11 +144,12 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
     } else if (isb) {
         S.b[ei] = a;
     }
-    const double residualSum = (double)(float)(mode == YAS_TRACK_RGB ? S.B[27] : S.A[27]);
-    const double numResidual = (double)(float)(mode == YAS_TRACK_ICP ? S.A[28] : S.A[29]);
+    // residualSum and numResidual are FP32 in the reference
+    const float residualSum = to_float_rn(mode == YAS_TRACK_RGB ? S.B[27] : S.A[27]);
+    const float numResidual = to_float_rn(mode == YAS_TRACK_ICP ? S.A[28] : S.A[29]);
     if (lane == 0) {
-        S.stats[0] = residualSum;
-        S.stats[1] = numResidual;
+        S.stats[0] = (double)residualSum;
+        S.stats[1] = (double)numResidual;
         S.stats[2] = (double)S.huber_th;
         S.stats[3] = S.A[28];
     }
@@ -141,59 +157,67 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
         __syncwarp();
         return;
     }
-    const float error = sqrtf((float)residualSum) / ((float)numResidual + 6.0f);
-    // ---- right-looking LDL^T with diagonal pivoting on [H | b]
+    // ---- LDL^T on [H | b] with a static pivot order: the diagonal's initial
+    // |values|, largest first (first on ties), applied as one symmetric
+    // permutation; the factorisation itself divides through the refined
+    // reciprocal of each pivot
     int orig = ei;  // b lanes: original index of the row they hold
     bool broke = false;
+    {
+        const unsigned long long ab0 = abs_bits(a);
+        const long long key0 = (ism && ei == ej) ? (ab0 > kInfBits ? -1LL : (long long)ab0) : -2LL;
+        long long kd[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        // pivot: largest |diagonal| over k..5, first on ties; a NaN never wins
-        // and a NaN at k keeps k; |doubles| order like their bit patterns
-        const unsigned long long ab = abs_bits(a);
-        const long long key = (ism && ei == ej) ? (ab > kInfBits ? -1LL : (long long)ab) : -2LL;
-        long long kq[6];
+        for (int q = 0; q < 6; ++q) kd[q] = __shfl_sync(kAll, key0, tri_lane(q, q));
+        int pos[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) kq[q] = __shfl_sync(kAll, key, tri_lane(q, q));
-        int p = k;
-        if (kq[k] >= 0) {
-            long long bestk = kq[k];
+        for (int q = 0; q < 6; ++q) {
+            int rq = 0;
 #pragma unroll
-            for (int q = k + 1; q < 6; ++q)
-                if (kq[q] > bestk) {
-                    bestk = kq[q];
-                    p = q;
-                }
+            for (int r = 0; r < 6; ++r) rq += (kd[r] > kd[q] || (kd[r] == kd[q] && r < q)) ? 1 : 0;
+            pos[q] = rq;
         }
-        if (p != k) {
-            // symmetric swap of k and p: element (i, j) <- (pi(i), pi(j))
-            const int si = ei == k ? p : (ei == p ? k : ei);
-            const int sj = ej == k ? p : (ej == p ? k : ej);
-            const int src = ism ? (si >= sj ? tri_lane(si, sj) : tri_lane(sj, si)) : (isb ? 21 + si : lane);
+        int inv[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) inv[pos[q]] = q;
+        // no factorisation when the largest diagonal is zero or the first is NaN
+        const long long kmax = kd[inv[0]];
+        broke = kmax <= 0 || kd[0] == -1LL;
+        if (!broke) {
+            const int pi = ism || isb ? inv[ei] : 0;
+            const int pj = ism ? inv[ej] : 0;
+            const int src = ism ? (pi >= pj ? tri_lane(pi, pj) : tri_lane(pj, pi)) : (isb ? 21 + pi : lane);
             a = __shfl_sync(kAll, a, src);
-            orig = __shfl_sync(kAll, orig, src);
+            if (isb) orig = pi;
         }
-        const double d = __shfl_sync(kAll, a, tri_lane(k, k));
-        const unsigned long long db = abs_bits(d);
-        const bool valid = db != 0ull && db <= kInfBits;
-        if (k == 0 && !valid) {
-            broke = true;  // identity transpositions, the matrix is used as it is
-            break;
+    }
+    if (!broke) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const bool upd = ei > k && ((ism && ej > k) || isb);
+            const int src_l = upd ? tri_lane(ei, k) : lane;
+            const int src_x = upd ? (isb ? 21 + k : tri_lane(ej, k)) : lane;
+            const double d = __shfl_sync(kAll, a, tri_lane(k, k));
+            const double lik = __shfl_sync(kAll, a, src_l);
+            const double ajk = __shfl_sync(kAll, a, src_x);
+            const unsigned long long db = abs_bits(d);
+            const bool valid = db != 0ull && db <= kInfBits;
+            const double t = lik * ajk;
+            double r = 1.0;  // undivided for a zero pivot
+            if (valid) {
+                if (seed_range(d)) {
+                    const double r0 = rcp_seed(d);
+                    r = fma(r0, fma(-d, r0, 1.0), r0);
+                } else {
+                    r = 1.0 / d;
+                }
+            }
+            const double na = fma(-t, r, a);
+            const bool colk = ism && ej == k && ei > k;
+            const double nl = a * r;
+            if (upd && (isb || valid)) a = na;
+            if (colk) a = nl;
         }
-        // l_ik = a_ik / d on the column-k lanes (undivided for a zero pivot)
-        const double l = valid ? div_seeded(a, d) : a;
-        const bool colk = ism && ej == k && ei > k;
-        // trailing update a_ij -= l_ik a_jk (i >= j > k), b_i -= l_ik b_k (i > k)
-        int src_l = lane, src_x = lane;
-        const bool upd = ei > k && ((ism && ej > k && valid) || isb);
-        if (upd) {
-            src_l = tri_lane(ei, k);
-            src_x = isb ? 21 + k : tri_lane(ej, k);
-        }
-        const double lik = __shfl_sync(kAll, l, src_l);
-        const double ajk = __shfl_sync(kAll, a, src_x);
-        const double na = fma(-lik, ajk, a);
-        if (upd) a = na;
-        if (colk) a = l;
     }
     if (broke) {  // forward substitution with the unfactored lower triangle
 #pragma unroll
@@ -241,12 +265,16 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
     const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
     double cA, cB, cC;
     if (abs_bits(th2) < 0x3f847ae147ae147bull) {  // th^2 < 1e-2
-        // Taylor series in th^2 to the th^8 term (truncation below 3e-18); lane
-        // r % 3 evaluates series r % 3
+        // Taylor series in th^2 to the th^8 term (truncation below 3e-18) of
+        // sin(th)/th, (1-cos th)/th^2 and (th-sin th)/th^3; lane r % 3
+        // evaluates series r % 3 (coefficients selected from immediates)
         const int sr = lane % 3;
-        const double pc = fma(th2, fma(th2, fma(th2, fma(th2, c_exp_poly[sr][4], c_exp_poly[sr][3]), c_exp_poly[sr][2]),
-                                       c_exp_poly[sr][1]),
-                              c_exp_poly[sr][0]);
+        const double p4 = sel3(sr, 1.0 / 362880.0, 1.0 / 3628800.0, 1.0 / 39916800.0);
+        const double p3 = sel3(sr, -1.0 / 5040.0, -1.0 / 40320.0, -1.0 / 362880.0);
+        const double p2 = sel3(sr, 1.0 / 120.0, 1.0 / 720.0, 1.0 / 5040.0);
+        const double p1 = sel3(sr, -1.0 / 6.0, -1.0 / 24.0, -1.0 / 120.0);
+        const double p0 = sel3(sr, 1.0, 0.5, 1.0 / 6.0);
+        const double pc = fma(th2, fma(th2, fma(th2, fma(th2, p4, p3), p2), p1), p0);
         cA = __shfl_sync(kAll, pc, 0);
         cB = __shfl_sync(kAll, pc, 1);
         cC = __shfl_sync(kAll, pc, 2);
@@ -283,6 +311,7 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
     const double E2 = __shfl_sync(kAll, ent, i * 4 + 2), ti = __shfl_sync(kAll, ent, i * 4 + 3);
     const double o = fma(E0, S.est[q], fma(E1, S.est[4 + q], fma(E2, S.est[8 + q], tl ? ti : 0.0)));
     // ---- acceptance on the error measured before the update
+    const float error = sqrtf(residualSum) / (numResidual + 6.0f);
     int accept = 0;
     if (lane == 0) {
         const double last = first_of_level ? (double)FLT_MAX : S.last_error;
