@@ -660,6 +660,44 @@ def run_large(frames: int = 2000):
             "loop_gap_first_last": {"t_m": round(loop[0], 4), "r_rad": round(loop[1], 4)}}
 
 
+def run_mesh(frames: int = 50, repeats: int = 3):
+    """Marching cubes over every allocated block of the map that a session
+    builds from the first `frames` frames of the benchmark's sequence
+    (640x480, 5 mm, FP16 words): the mesher's count, scan and emit kernels on
+    a realistic map.  Reports blocks, triangles and the wall time of each
+    meshing after a warm call (synchronised on both sides)."""
+    import ctypes as C
+
+    import torch
+
+    from yetanotherslam_gb300 import _lib as L
+    from yetanotherslam_gb300 import rgbdfusion as rf
+    from yetanotherslam_gb300 import synth
+
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    K = synth.intrinsics(W, H)
+    fr = make_frames(frames, W, H, WORKLOAD["scene_seed"])
+    s = rf.Session(W, H, K, hash_slots=WORKLOAD["hash_slots"], max_blocks=WORKLOAD["max_blocks"],
+                   voxel_size=WORKLOAD["voxel_m"], trunc_dist=WORKLOAD["trunc_m"], voxel_format=rf.VOXEL_F16,
+                   num_levels=3, iterations=GN_ITERS)
+    bad = sum(int(s.process(f.rgb, f.depth)[0] != 0) for f in fr)
+    m = s.map()
+    me = rf.MeshEngine(8_000_000)
+    ntri = C.c_uint()
+    L.call("yas_mesher_meshify", me.handle, m.handle, C.byref(ntri))  # warm
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        L.call("yas_mesher_meshify", me.handle, m.handle, C.byref(ntri))
+        torch.cuda.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+    out = {"frames": frames, "frame_status_nonzero": bad, "blocks": m.num_allocated(), "triangles": ntri.value,
+           "mesh_ms": [round(x, 3) for x in ms]}
+    s.close()
+    return out
+
+
 def se3_exp_np(xi):
     """exp of a twist (translation part, rotation part) as a 4x4 matrix (Rodrigues and the left Jacobian)."""
     v, w = np.asarray(xi[:3], float), np.asarray(xi[3:], float)
@@ -831,7 +869,7 @@ def main():
     ap.add_argument("--batched", type=int, default=1, help="1: also measure 16 batched submaps (C3)")
     ap.add_argument("--large", type=int, default=1, help="1: also run the 2000-frame 1280x720 large map (C5)")
     ap.add_argument("--large-frames", type=int, default=2000)
-    ap.add_argument("--leg", choices=["served", "batched", "batched-pass", "large"], default=None,
+    ap.add_argument("--leg", choices=["served", "batched", "batched-pass", "large", "mesh"], default=None,
                     help="run only this workload and print its result (for profiling one leg)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -839,7 +877,7 @@ def main():
     if args.leg:
         fn = {"served": lambda: run_served(100, args.served_gn, args.served_ppc), "batched": lambda: run_batched(7),
               "batched-pass": lambda: run_batched(7, only_pass=True),
-              "large": lambda: run_large(args.large_frames)}[args.leg]
+              "large": lambda: run_large(args.large_frames), "mesh": lambda: run_mesh()}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn()}))
         return
     if args.impl == "reference":

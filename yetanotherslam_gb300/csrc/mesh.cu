@@ -21,8 +21,9 @@
 // GB300 design: one CTA per block stages the 9x9x9 sdf neighbourhood in shared
 // memory (own block with 16-byte loads plus the +x/+y/+z halo from up to 7
 // neighbour blocks); pass 1 counts triangles per block, a scan assigns each
-// block a contiguous output range, pass 2 re-derives the per-thread offsets
-// and writes the soup, so the output order is a pure function of the map.
+// block a contiguous output range, pass 2 scans the block's cube counts and
+// writes one triangle per thread, so the output order (cube order, then table
+// order) is a pure function of the map.
 #include <cstring>
 
 #include "yas_internal.h"
@@ -199,16 +200,22 @@ __device__ __forceinline__ int cube_case(const float *s, int x, int y, int z, fl
     return cidx;
 }
 
-__device__ __forceinline__ int cube_tris(int cidx) {
-    if (cidx <= 0) return 0;
-    if (c_edge_table[cidx] == 0) return 0;
-    return c_tri_count[cidx];
+// Triangles of a case, from a shared-memory copy of the count table (zero for
+// the cases without crossings): lanes with different cases do not serialise.
+__device__ __forceinline__ int cube_tris(int cidx, const unsigned char *count) {
+    return cidx <= 0 ? 0 : (int)count[cidx];
+}
+
+__device__ __forceinline__ void load_counts(unsigned char *count) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) count[i] = c_edge_table[i] == 0 ? 0 : c_tri_count[i];
 }
 
 template <int FMT>
 __global__ void __launch_bounds__(128) mc_count_kernel(MapDev m, unsigned nblocks, unsigned *block_tris) {
     __shared__ float s[kN3];
     __shared__ unsigned red[4];
+    __shared__ unsigned char count[256];
+    load_counts(count);  // visible after stage_block's barrier
     for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
         int bx, by, bz;
         unpack_key(m.block_keys[b], bx, by, bz);
@@ -216,7 +223,7 @@ __global__ void __launch_bounds__(128) mc_count_kernel(MapDev m, unsigned nblock
         unsigned cnt = 0;
         for (int i = threadIdx.x; i < kBlockVoxels; i += blockDim.x) {
             float sd[8];
-            cnt += cube_tris(cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd));
+            cnt += cube_tris(cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd), count);
         }
         for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
@@ -291,84 +298,107 @@ __device__ __forceinline__ float3 edge_vertex(int e, const float sd[8], float px
     }
 }
 
+// Emission: one CTA per block (grid-stride), one thread per triangle.  The
+// CTA stages the block's 9^3 neighbourhood, forms every cube's case and
+// triangle count, scans the counts in cube order, then thread j writes the
+// block's triangles j, j + 128, ...: a binary search over the scan finds the
+// triangle's cube, so consecutive threads write consecutive triangles (the
+// soup's order is cube order, then table order: a pure function of the map).
+// The triangle table is read from a shared-memory copy, so the lanes of a warp
+// look up different cases without serialising on the constant cache.
 template <int FMT>
 __global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks,
                                                       const unsigned *block_offset, int max_tris,
                                                       float *points, float *normals, int *cases,
                                                       int *cube_xyz) {
     __shared__ float s[kN3];
+    __shared__ signed char tri[256][kMcMaxTriIdx];
+    __shared__ unsigned short pre[kBlockVoxels + 1];  // exclusive prefix of the cubes' triangle counts
     __shared__ unsigned wsum[4];
+    __shared__ unsigned char count[256];
+    for (int i = threadIdx.x; i < 256 * kMcMaxTriIdx; i += blockDim.x) (&tri[0][0])[i] = (&c_tri_table[0][0])[i];
+    load_counts(count);
     const float vs = m.voxel_size;
     for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
         const unsigned base = block_offset[b];
-        if (block_offset[b + 1] == base) continue;  // uniform across the CTA
+        const unsigned ntri = block_offset[b + 1] - base;
+        if (ntri == 0) continue;  // uniform across the CTA
         int bx, by, bz;
         unpack_key(m.block_keys[b], bx, by, bz);
-        stage_block<FMT>(m, (int)b, bx, by, bz, s);
-        // each thread owns 4 consecutive cubes: i = 4*tid .. 4*tid+3
-        int cnt[4], cid[4];
+        stage_block<FMT>(m, (int)b, bx, by, bz, s);  // ends with a barrier (also for the table copies)
+        // triangle counts of the thread's 4 consecutive cubes, scanned over the CTA
+        int cnt[4];
         unsigned mine = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            int i = threadIdx.x * 4 + k;
+            const int i = threadIdx.x * 4 + k;
             float sd[8];
-            cid[k] = cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd);
-            cnt[k] = cube_tris(cid[k]);
-            mine += cnt[k];
+            cnt[k] = cube_tris(cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd), count);
+            mine += (unsigned)cnt[k];
         }
         unsigned incl = mine;
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
             if ((threadIdx.x & 31) >= (unsigned)o) incl += y;
         }
         if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = incl;
         __syncthreads();
-        unsigned wpre = 0;
-        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) wpre += wsum[w];
-        unsigned off = base + wpre + incl - mine;
-#pragma unroll 1
+        unsigned run = incl - mine;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) run += wsum[w];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if (cnt[k] == 0) continue;
-            int i = threadIdx.x * 4 + k;
-            int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
+            pre[threadIdx.x * 4 + k] = (unsigned short)run;
+            run += (unsigned)cnt[k];
+        }
+        if (threadIdx.x == blockDim.x - 1) pre[kBlockVoxels] = (unsigned short)run;
+        __syncthreads();
+        for (unsigned j = threadIdx.x; j < ntri; j += blockDim.x) {
+            const unsigned off = base + j;
+            if (off >= (unsigned)max_tris) break;
+            // the cube i with pre[i] <= j < pre[i + 1]
+            int lo = 0, hi = kBlockVoxels - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if ((unsigned)pre[mid] <= j) lo = mid;
+                else hi = mid - 1;
+            }
+            const int i = lo, t = (int)(j - pre[i]);
+            const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
             float sd[8];
-            cube_case(s, lx, ly, lz, sd);
+            const int c = cube_case(s, lx, ly, lz, sd);
             const int gx = bx * 8 + lx, gy = by * 8 + ly, gz = bz * 8 + lz;
             const float px = (float)gx, py = (float)gy, pz = (float)gz;
-            for (int t = 0; t < cnt[k]; ++t, ++off) {
-                if (off >= (unsigned)max_tris) continue;
-                float3 v[3];
+            float3 v[3];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    float3 q = edge_vertex(c_tri_table[cid[k]][3 * t + j], sd, px, py, pz);
-                    v[j] = make_float3(q.x * vs, q.y * vs, q.z * vs);
-                }
-                float ax = v[1].x - v[0].x, ay = v[1].y - v[0].y, az = v[1].z - v[0].z;
-                float cx = v[2].x - v[0].x, cy = v[2].y - v[0].y, cz = v[2].z - v[0].z;
-                float nx = ay * cz - az * cy, ny = az * cx - ax * cz, nz = ax * cy - ay * cx;
-                float nn = nx * nx + ny * ny + nz * nz;
-                if (nn > 0.0f) {
-                    float inv = 1.0f / sqrtf(nn);
-                    nx *= inv;
-                    ny *= inv;
-                    nz *= inv;
-                }
-                float *pp = points + (size_t)off * 9;
-                float *nq = normals + (size_t)off * 9;
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    pp[3 * j] = v[j].x;
-                    pp[3 * j + 1] = v[j].y;
-                    pp[3 * j + 2] = v[j].z;
-                    nq[3 * j] = nx;
-                    nq[3 * j + 1] = ny;
-                    nq[3 * j + 2] = nz;
-                }
-                cases[off] = cid[k];
-                cube_xyz[3 * off] = gx;
-                cube_xyz[3 * off + 1] = gy;
-                cube_xyz[3 * off + 2] = gz;
+            for (int q = 0; q < 3; ++q) {
+                const float3 e = edge_vertex(tri[c][3 * t + q], sd, px, py, pz);
+                v[q] = make_float3(e.x * vs, e.y * vs, e.z * vs);
             }
+            const float ax = v[1].x - v[0].x, ay = v[1].y - v[0].y, az = v[1].z - v[0].z;
+            const float cx = v[2].x - v[0].x, cy = v[2].y - v[0].y, cz = v[2].z - v[0].z;
+            float nx = ay * cz - az * cy, ny = az * cx - ax * cz, nz = ax * cy - ay * cx;
+            const float nn = nx * nx + ny * ny + nz * nz;
+            if (nn > 0.0f) {
+                const float inv = 1.0f / sqrtf(nn);
+                nx *= inv;
+                ny *= inv;
+                nz *= inv;
+            }
+            float *pp = points + (size_t)off * 9;
+            float *nq = normals + (size_t)off * 9;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                pp[3 * q] = v[q].x;
+                pp[3 * q + 1] = v[q].y;
+                pp[3 * q + 2] = v[q].z;
+                nq[3 * q] = nx;
+                nq[3 * q + 1] = ny;
+                nq[3 * q + 2] = nz;
+            }
+            cases[off] = c;
+            cube_xyz[3 * off] = gx;
+            cube_xyz[3 * off + 1] = gy;
+            cube_xyz[3 * off + 2] = gz;
         }
         __syncthreads();
     }
