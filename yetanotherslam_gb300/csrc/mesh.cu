@@ -279,50 +279,59 @@ __device__ __forceinline__ float mc_interp(float v1, float v2) {
     return (0.0f - v1) / (v2 - v1);
 }
 
-// Vertex on edge e of the cube at voxel position (px,py,pz), voxel units
-// (MeshEngine.cu:151-225).
-__device__ __forceinline__ float3 edge_vertex(int e, const float sd[8], float px, float py, float pz) {
-    switch (e) {
-        case 0: return make_float3(px + mc_interp(sd[0], sd[1]), py, pz);
-        case 1: return make_float3(px + 1.0f, py + mc_interp(sd[1], sd[2]), pz);
-        case 2: return make_float3(px + (1.0f - mc_interp(sd[2], sd[3])), py + 1.0f, pz);
-        case 3: return make_float3(px, py + (1.0f - mc_interp(sd[3], sd[0])), pz);
-        case 4: return make_float3(px + mc_interp(sd[4], sd[5]), py, pz + 1.0f);
-        case 5: return make_float3(px + 1.0f, py + mc_interp(sd[5], sd[6]), pz + 1.0f);
-        case 6: return make_float3(px + (1.0f - mc_interp(sd[6], sd[7])), py + 1.0f, pz + 1.0f);
-        case 7: return make_float3(px, py + (1.0f - mc_interp(sd[7], sd[4])), pz + 1.0f);
-        case 8: return make_float3(px, py, pz + mc_interp(sd[0], sd[4]));
-        case 9: return make_float3(px + 1.0f, py, pz + mc_interp(sd[1], sd[5]));
-        case 10: return make_float3(px + 1.0f, py + 1.0f, pz + mc_interp(sd[2], sd[6]));
-        default: return make_float3(px, py + 1.0f, pz + mc_interp(sd[3], sd[7]));
-    }
+// Emission: one CTA per block (grid-stride), one thread per triangle.  The
+// CTA stages the block's 9^3 neighbourhood, forms every cube's triangle count,
+// scans the counts in cube order and lists (cube, triangle) per output slot;
+// thread j then writes the block's triangles j, j + 128, ..., so consecutive
+// threads write consecutive triangles.  The soup's order is cube order, then
+// table order: a pure function of the map.  The triangle and
+// count tables are read from shared-memory copies, so the lanes of a warp look
+// up different cases without serialising on the constant cache.
+constexpr int kEmitThreads = 128;
+constexpr int kMaxBlockTris = kBlockVoxels * ((kMcMaxTriIdx - 1) / 3);  // 5120
+
+// Vertex on edge e of the cube at local (lx,ly,lz), voxel position (px,py,pz),
+// in voxel units: the reference's per-edge interpolation from the edge's first
+// corner (MeshEngine.cu:151-225), driven by the edge and corner tables instead
+// of a switch over the 12 edges, so the lanes of a warp on different edges do
+// not diverge.  Along the
+// edge's axis the coordinate is p + (a + t (b - a)) for corner coordinates a,
+// b in {0, 1}, which is p + t or p + (1 - t) exactly as the per-edge forms.
+__device__ __forceinline__ float3 edge_vertex_tab(int e, const float *s, int lx, int ly, int lz, float px, float py,
+                                                  float pz) {
+    // corners a, b of edge e (kEdge) as nibble e of two constants; corner c's
+    // offset (kCorner): dx = bit c of 0x66, dy = bit c of 0xcc, dz = c >> 2
+    const int a = (int)((0x321076543210ull >> (4 * e)) & 15ull);
+    const int b = (int)((0x765447650321ull >> (4 * e)) & 15ull);
+    const int ax = (0x66 >> a) & 1, ay = (0xcc >> a) & 1, az = a >> 2;
+    const int bx = (0x66 >> b) & 1, by = (0xcc >> b) & 1, bz = b >> 2;
+    const float va = s[(lz + az) * 81 + (ly + ay) * 9 + (lx + ax)];
+    const float vb = s[(lz + bz) * 81 + (ly + by) * 9 + (lx + bx)];
+    const float t = mc_interp(va, vb);
+    const float ox = ax == bx ? (float)ax : (float)ax + t * (float)(bx - ax);
+    const float oy = ay == by ? (float)ay : (float)ay + t * (float)(by - ay);
+    const float oz = az == bz ? (float)az : (float)az + t * (float)(bz - az);
+    return make_float3(px + ox, py + oy, pz + oz);
 }
 
-// Emission: one CTA per block (grid-stride), one thread per triangle.  The
-// CTA stages the block's 9^3 neighbourhood, forms every cube's case and
-// triangle count, scans the counts in cube order, then thread j writes the
-// block's triangles j, j + 128, ...: a binary search over the scan finds the
-// triangle's cube, so consecutive threads write consecutive triangles (the
-// soup's order is cube order, then table order: a pure function of the map).
-// The triangle table is read from a shared-memory copy, so the lanes of a warp
-// look up different cases without serialising on the constant cache.
 template <int FMT>
-__global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks,
-                                                      const unsigned *block_offset, int max_tris,
-                                                      float *points, float *normals, int *cases,
-                                                      int *cube_xyz) {
+__global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(MapDev m, unsigned nblocks,
+                                                               const unsigned *block_offset, int max_tris,
+                                                               float *points, float *normals, int *cases,
+                                                               int *cube_xyz) {
     __shared__ float s[kN3];
     __shared__ signed char tri[256][kMcMaxTriIdx];
-    __shared__ unsigned short pre[kBlockVoxels + 1];  // exclusive prefix of the cubes' triangle counts
-    __shared__ unsigned wsum[4];
     __shared__ unsigned char count[256];
+    __shared__ unsigned short slot[kMaxBlockTris];  // output slot -> cube << 4 | triangle of the cube
+    __shared__ unsigned char ucase[kBlockVoxels];  // case index of each cube with triangles
+    __shared__ unsigned wsum[kEmitThreads / 32];
     for (int i = threadIdx.x; i < 256 * kMcMaxTriIdx; i += blockDim.x) (&tri[0][0])[i] = (&c_tri_table[0][0])[i];
     load_counts(count);
     const float vs = m.voxel_size;
     for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
         const unsigned base = block_offset[b];
         const unsigned ntri = block_offset[b + 1] - base;
-        if (ntri == 0) continue;  // uniform across the CTA
+        if (ntri == 0 || base >= (unsigned)max_tris) continue;  // uniform across the CTA
         int bx, by, bz;
         unpack_key(m.block_keys[b], bx, by, bz);
         stage_block<FMT>(m, (int)b, bx, by, bz, s);  // ends with a barrier (also for the table copies)
@@ -333,7 +342,9 @@ __global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks
         for (int k = 0; k < 4; ++k) {
             const int i = threadIdx.x * 4 + k;
             float sd[8];
-            cnt[k] = cube_tris(cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd), count);
+            const int c = cube_case(s, i & 7, (i >> 3) & 7, i >> 6, sd);
+            cnt[k] = cube_tris(c, count);
+            ucase[i] = (unsigned char)(c < 0 ? 0 : c);
             mine += (unsigned)cnt[k];
         }
         unsigned incl = mine;
@@ -347,32 +358,24 @@ __global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks
         for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) run += wsum[w];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            pre[threadIdx.x * 4 + k] = (unsigned short)run;
+            const unsigned i = threadIdx.x * 4 + k;
+            for (int t = 0; t < cnt[k]; ++t) slot[run + t] = (unsigned short)(i << 4 | (unsigned)t);
             run += (unsigned)cnt[k];
         }
-        if (threadIdx.x == blockDim.x - 1) pre[kBlockVoxels] = (unsigned short)run;
         __syncthreads();
-        for (unsigned j = threadIdx.x; j < ntri; j += blockDim.x) {
-            const unsigned off = base + j;
-            if (off >= (unsigned)max_tris) break;
-            // the cube i with pre[i] <= j < pre[i + 1]
-            int lo = 0, hi = kBlockVoxels - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if ((unsigned)pre[mid] <= j) lo = mid;
-                else hi = mid - 1;
-            }
-            const int i = lo, t = (int)(j - pre[i]);
+        const unsigned nout = min(ntri, (unsigned)max_tris - base);
+        for (unsigned j = threadIdx.x; j < nout; j += kEmitThreads) {
+            const unsigned e = slot[j];
+            const int i = (int)(e >> 4), t = (int)(e & 15u);
             const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
-            float sd[8];
-            const int c = cube_case(s, lx, ly, lz, sd);
+            const int c = ucase[i];
             const int gx = bx * 8 + lx, gy = by * 8 + ly, gz = bz * 8 + lz;
             const float px = (float)gx, py = (float)gy, pz = (float)gz;
             float3 v[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                const float3 e = edge_vertex(tri[c][3 * t + q], sd, px, py, pz);
-                v[q] = make_float3(e.x * vs, e.y * vs, e.z * vs);
+                const float3 ev = edge_vertex_tab(tri[c][3 * t + q], s, lx, ly, lz, px, py, pz);
+                v[q] = make_float3(ev.x * vs, ev.y * vs, ev.z * vs);
             }
             const float ax = v[1].x - v[0].x, ay = v[1].y - v[0].y, az = v[1].z - v[0].z;
             const float cx = v[2].x - v[0].x, cy = v[2].y - v[0].y, cz = v[2].z - v[0].z;
@@ -384,8 +387,9 @@ __global__ void __launch_bounds__(128) mc_emit_kernel(MapDev m, unsigned nblocks
                 ny *= inv;
                 nz *= inv;
             }
-            float *pp = points + (size_t)off * 9;
-            float *nq = normals + (size_t)off * 9;
+            const size_t off = (size_t)base + j;
+            float *pp = points + off * 9;
+            float *nq = normals + off * 9;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 pp[3 * q] = v[q].x;
@@ -443,19 +447,19 @@ int launch_meshify(const MapDev &m, int fmt, MeshBuffers &mb, unsigned n_blocks,
     scan_kernel<<<1, 1024, 0, s>>>(mb.block_tris, mb.block_offset, n_blocks, mb.counters);
     switch (fmt) {
         case YAS_VOXEL_F32:
-            mc_emit_kernel<YAS_VOXEL_F32><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+            mc_emit_kernel<YAS_VOXEL_F32><<<grid, kEmitThreads, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
                                                                mb.points, mb.normals, mb.cases, mb.cube_xyz);
             break;
         case YAS_VOXEL_F16:
-            mc_emit_kernel<YAS_VOXEL_F16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+            mc_emit_kernel<YAS_VOXEL_F16><<<grid, kEmitThreads, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
                                                                mb.points, mb.normals, mb.cases, mb.cube_xyz);
             break;
         case YAS_VOXEL_S16:
-            mc_emit_kernel<YAS_VOXEL_S16><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+            mc_emit_kernel<YAS_VOXEL_S16><<<grid, kEmitThreads, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
                                                                mb.points, mb.normals, mb.cases, mb.cube_xyz);
             break;
         default:
-            mc_emit_kernel<YAS_VOXEL_S24><<<grid, 128, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
+            mc_emit_kernel<YAS_VOXEL_S24><<<grid, kEmitThreads, 0, s>>>(m, n_blocks, mb.block_offset, mb.max_tris,
                                                                mb.points, mb.normals, mb.cases, mb.cube_xyz);
             break;
     }
