@@ -18,6 +18,7 @@
 //   model pyramid          RGBDTracking.cu:140-150 (SetReferenceModel); the reference runs
 //                          the float pyr-down on the float4 model (its coarse model levels
 //                          are unusable); here the intended float4 nearest pyr-down is used.
+#include <cstring>
 #include <type_traits>
 
 #include "yas_internal.h"
@@ -182,31 +183,57 @@ __global__ void depth_pyr_kernel(const float *__restrict__ prev, int pw, LevelCa
     nmap[y * c.w + x] = n;
 }
 
-// Model level 0 normals (vmap given) or level l >= 1 vmap + normals from l-1.
-__device__ __forceinline__ float4 vmap_down(const float4 *prev, int pw, int x, int y, int w, int h) {
-    if (x >= w - 1 || y >= h - 1) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-    return prev[(size_t)(2 * y) * pw + 2 * x];
+// The whole model pyramid in one launch (RGBDTracking.cu:140-150: level 0's
+// normals, then each level's nearest pyr-down vertex map and its normals).
+// Level l's vertex (x, y) of the chained pyr-down is level 0's vertex
+// (2^l x, 2^l y) when x < w_l - 1 and y < h_l - 1 and invalid otherwise (the
+// inner levels' conditions follow from the outer one), so every level reads
+// the raycast's level-0 map directly and no level waits for another: the same
+// values, one launch instead of one per level.  Thread i covers pixel i of the
+// levels laid end to end.
+struct ModelPyramid {
+    int L, w[kMaxLevels], h[kMaxLevels], first[kMaxLevels + 1];
+    float4 *vmap[kMaxLevels], *nmap[kMaxLevels];
+};
+
+__device__ __forceinline__ float4 model_vertex(const ModelPyramid &mp, int l, int x, int y) {
+    if (l == 0) {
+        if (x >= mp.w[0] || y >= mp.h[0]) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        return mp.vmap[0][(size_t)y * mp.w[0] + x];
+    }
+    if (x >= mp.w[l] - 1 || y >= mp.h[l] - 1) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    return mp.vmap[0][(size_t)(y << l) * mp.w[0] + (x << l)];
 }
 
-__global__ void model_level_kernel(const float4 *__restrict__ prev, int pw, int w, int h, float4 *vmap,
-                                   float4 *nmap) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h) return;
-    float4 v00, v01, v10;
-    if (prev == nullptr) {  // level 0: vmap already in place
-        v00 = vmap[y * w + x];
-        v01 = x < w - 1 ? vmap[y * w + x + 1] : make_float4(0, 0, 0, -1);
-        v10 = y < h - 1 ? vmap[(y + 1) * w + x] : make_float4(0, 0, 0, -1);
-    } else {
-        v00 = vmap_down(prev, pw, x, y, w, h);
-        v01 = vmap_down(prev, pw, x + 1, y, w, h);
-        v10 = vmap_down(prev, pw, x, y + 1, w, h);
-        vmap[y * w + x] = v00;
-    }
+__global__ void model_pyramid_kernel(const ModelPyramid mp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= mp.first[mp.L]) return;
+    int l = 0;
+    while (l + 1 < mp.L && i >= mp.first[l + 1]) ++l;
+    const int k = i - mp.first[l], w = mp.w[l], h = mp.h[l];
+    const int y = k / w, x = k - y * w;
+    const float4 v00 = model_vertex(mp, l, x, y);
+    if (l > 0) mp.vmap[l][k] = v00;
     float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-    if (x < w - 1 && y < h - 1) n = normal_of(v00, v01, v10);
-    nmap[y * w + x] = n;
+    if (x < w - 1 && y < h - 1) n = normal_of(v00, model_vertex(mp, l, x + 1, y), model_vertex(mp, l, x, y + 1));
+    mp.nmap[l][k] = n;
+}
+
+void launch_model_pyramid(int L, const int *w, const int *h, float4 *const *vmap, float4 *const *nmap,
+                          cudaStream_t s) {
+    ModelPyramid mp;
+    memset(&mp, 0, sizeof(mp));
+    mp.L = L;
+    mp.first[0] = 0;
+    for (int l = 0; l < L; ++l) {
+        mp.w[l] = w[l];
+        mp.h[l] = h[l];
+        mp.vmap[l] = vmap[l];
+        mp.nmap[l] = nmap[l];
+        mp.first[l + 1] = mp.first[l] + w[l] * h[l];
+    }
+    if (mp.first[L] == 0) return;
+    model_pyramid_kernel<<<(mp.first[L] + 255) / 256, 256, 0, s>>>(mp);
 }
 
 static dim3 grid2(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
@@ -231,11 +258,6 @@ void launch_depth_level0(const void *src, int is_u16, int pitch, float scale, co
 void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float4 *vmap,
                         float4 *nmap, cudaStream_t s) {
     depth_pyr_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(prev, pw, c, invd, vmap, nmap);
-}
-
-void launch_model_level(const float4 *prev, int pw, int w, int h, float4 *vmap, float4 *nmap,
-                        cudaStream_t s) {
-    model_level_kernel<<<grid2(w, h), dim3(32, 8), 0, s>>>(prev, pw, w, h, vmap, nmap);
 }
 
 // ---------------------------------------------------------------- shading

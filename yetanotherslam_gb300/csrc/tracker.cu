@@ -1240,10 +1240,15 @@ void tracker_depth(yas_tracker *tr, const void *src, int is_u16, int pitch, floa
 
 void tracker_model(yas_tracker *tr, cudaStream_t s) {
     TrackLevelBufs *B = tr->set[1 - tr->cur];
-    launch_model_level(nullptr, 0, tr->cam[0].w, tr->cam[0].h, B[0].vmap, B[0].nmap, s);
-    for (int l = 1; l < tr->L; ++l)
-        launch_model_level(B[l - 1].vmap, tr->cam[l - 1].w, tr->cam[l].w, tr->cam[l].h, B[l].vmap, B[l].nmap,
-                           s);
+    int w[kMaxLevels], h[kMaxLevels];
+    float4 *vm[kMaxLevels], *nm[kMaxLevels];
+    for (int l = 0; l < tr->L; ++l) {
+        w[l] = tr->cam[l].w;
+        h[l] = tr->cam[l].h;
+        vm[l] = B[l].vmap;
+        nm[l] = B[l].nmap;
+    }
+    launch_model_pyramid(tr->L, w, h, vm, nm, s);
 }
 
 }  // namespace yas

@@ -89,8 +89,8 @@ void launch_depth_level0(const void *src, int is_u16, int pitch, float scale, co
                          float *depth_m, float *invd, float4 *vmap, float4 *nmap, cudaStream_t s);
 void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float4 *vmap,
                         float4 *nmap, cudaStream_t s);
-void launch_model_level(const float4 *prev, int pw, int w, int h, float4 *vmap, float4 *nmap,
-                        cudaStream_t s);
+void launch_model_pyramid(int L, const int *w, const int *h, float4 *const *vmap, float4 *const *nmap,
+                          cudaStream_t s);
 void launch_render_scene(const float4 *vmap, const float4 *nmap, int vpitch, int w, int h, float3 light,
                          uchar4 *out, int opitch, cudaStream_t s);
 
