@@ -33,9 +33,12 @@ namespace yas {
 // ---------------------------------------------------------------- tables
 constexpr int kMcMaxTriIdx = 31;  // up to 10 triangles + terminator
 
-__constant__ unsigned short c_edge_table[256];
-__constant__ signed char c_tri_table[256][kMcMaxTriIdx];
-__constant__ unsigned char c_tri_count[256];
+// The tables in global memory: each CTA copies them into shared memory with
+// coalesced 16-byte loads (a constant-memory copy would serialise the lanes'
+// distinct addresses).  g_mc_count is 0 for the cases without crossings.
+__device__ __align__(16) signed char g_mc_tri[256 * kMcMaxTriIdx];
+__device__ __align__(16) unsigned char g_mc_count[256];
+static_assert((256 * kMcMaxTriIdx) % 16 == 0, "16-byte copies of the triangle table");
 
 static const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
@@ -145,9 +148,10 @@ void mesh_tables_upload() {
         build_mc_tables(tables);
         built = true;
     }
-    cudaMemcpyToSymbol(c_edge_table, tables.edge, sizeof(tables.edge));
-    cudaMemcpyToSymbol(c_tri_table, tables.tri, sizeof(tables.tri));
-    cudaMemcpyToSymbol(c_tri_count, tables.count, sizeof(tables.count));
+    unsigned char count[256];
+    for (int c = 0; c < 256; ++c) count[c] = tables.edge[c] == 0 ? 0 : tables.count[c];
+    cudaMemcpyToSymbol(g_mc_tri, tables.tri, sizeof(tables.tri));
+    cudaMemcpyToSymbol(g_mc_count, count, sizeof(count));
     // the copies run on the legacy stream; the engines launch on
     // non-blocking streams, which do not wait for it
     cudaStreamSynchronize(cudaStreamLegacy);
@@ -170,16 +174,34 @@ __device__ void stage_block(const MapDev &m, int b, int bx, int by, int bz, floa
     }
     __syncthreads();
     const float qnan = __int_as_float(0x7fffffff);
-    for (int i = threadIdx.x; i < kN3; i += blockDim.x) {
-        int x = i % kN, y = (i / kN) % kN, z = i / (kN * kN);
-        int c = (x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2);
-        int p = nb[c];
+    // the block's own 512 voxels: 16-byte loads of consecutive words (the pool
+    // is 16-byte aligned and a block's words are contiguous, z*64 + y*8 + x)
+    constexpr int kPer = 16 / (int)sizeof(typename IO::T);
+    const int4 *own = reinterpret_cast<const int4 *>(vox + (size_t)b * kBlockVoxels);
+    for (int q = threadIdx.x; q < kBlockVoxels / kPer; q += blockDim.x) {
+        const int4 w = __ldg(own + q);
+        const typename IO::T *e = reinterpret_cast<const typename IO::T *>(&w);
+        const int i0 = q * kPer, x = i0 & 7, y = (i0 >> 3) & 7, z = i0 >> 6;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) s[z * 81 + y * 9 + x + j] = IO::wt(e[j]) != 0 ? IO::sdf(e[j]) : qnan;
+    }
+    // the 217 halo cells (x, y or z = 8) from the +x / +y / +z neighbours
+    for (int h = threadIdx.x; h < kN3 - kBlockVoxels; h += blockDim.x) {
+        int x, y, z;
+        if (h < 81) {  // x = 8: y, z in 0..8
+            x = 8, y = h % 9, z = h / 9;
+        } else if (h < 153) {  // y = 8: x in 0..7, z in 0..8
+            x = (h - 81) & 7, y = 8, z = (h - 81) >> 3;
+        } else {  // z = 8: x, y in 0..7
+            x = (h - 153) & 7, y = (h - 153) >> 3, z = 8;
+        }
+        const int p = nb[(x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2)];
         float v = qnan;
         if (p >= 0) {
-            typename IO::T r = __ldg(vox + (size_t)p * kBlockVoxels + ((z & 7) << 6) + ((y & 7) << 3) + (x & 7));
+            const typename IO::T r = __ldg(vox + (size_t)p * kBlockVoxels + ((z & 7) << 6) + ((y & 7) << 3) + (x & 7));
             if (IO::wt(r) != 0) v = IO::sdf(r);
         }
-        s[i] = v;
+        s[z * 81 + y * 9 + x] = v;
     }
     __syncthreads();
 }
@@ -207,14 +229,15 @@ __device__ __forceinline__ int cube_tris(int cidx, const unsigned char *count) {
 }
 
 __device__ __forceinline__ void load_counts(unsigned char *count) {
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) count[i] = c_edge_table[i] == 0 ? 0 : c_tri_count[i];
+    for (int i = threadIdx.x; i < 16; i += blockDim.x)
+        reinterpret_cast<int4 *>(count)[i] = reinterpret_cast<const int4 *>(g_mc_count)[i];
 }
 
 template <int FMT>
 __global__ void __launch_bounds__(128) mc_count_kernel(MapDev m, unsigned nblocks, unsigned *block_tris) {
     __shared__ float s[kN3];
     __shared__ unsigned red[4];
-    __shared__ unsigned char count[256];
+    __shared__ __align__(16) unsigned char count[256];
     load_counts(count);  // visible after stage_block's barrier
     for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
         int bx, by, bz;
@@ -233,42 +256,43 @@ __global__ void __launch_bounds__(128) mc_count_kernel(MapDev m, unsigned nblock
     }
 }
 
-// Exclusive scan of per-block counts (single CTA; offsets[n] = total).
+// Exclusive scan of per-block counts (single CTA; offsets[n] = total).  Thread
+// t owns the contiguous run [t * per, (t + 1) * per): it sums its run, the CTA
+// scans the 1024 run sums once, and the thread writes its run's prefixes, so
+// the CTA synchronises a fixed number of times whatever n is.
 __global__ void __launch_bounds__(1024) scan_kernel(const unsigned *in, unsigned *out, unsigned n,
                                                     unsigned *total) {
     __shared__ unsigned warp_sums[32];
-    __shared__ unsigned carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (unsigned base = 0; base < n; base += blockDim.x) {
-        unsigned i = base + threadIdx.x;
-        unsigned v = i < n ? in[i] : 0u;
-        unsigned x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if ((threadIdx.x & 31) >= (unsigned)o) x += y;
-        }
-        if ((threadIdx.x & 31) == 31) warp_sums[threadIdx.x >> 5] = x;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            unsigned w = warp_sums[threadIdx.x];
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-                if (threadIdx.x >= (unsigned)o) w += y;
-            }
-            warp_sums[threadIdx.x] = w;
-        }
-        __syncthreads();
-        unsigned wprefix = (threadIdx.x >= 32) ? warp_sums[(threadIdx.x >> 5) - 1] : 0u;
-        unsigned incl = x + wprefix;
-        if (i < n) out[i] = carry + incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry += incl;
-        __syncthreads();
+    const unsigned per = (n + blockDim.x - 1) / blockDim.x;
+    const unsigned lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+    unsigned sum = 0;
+    for (unsigned i = lo; i < hi; ++i) sum += in[i];
+    unsigned x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) >= (unsigned)o) x += y;
     }
-    if (threadIdx.x == 0) {
-        out[n] = carry;
-        *total = carry;
+    if ((threadIdx.x & 31) == 31) warp_sums[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned w = warp_sums[threadIdx.x];
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (threadIdx.x >= (unsigned)o) w += y;
+        }
+        warp_sums[threadIdx.x] = w;
+    }
+    __syncthreads();
+    unsigned run = x - sum + ((threadIdx.x >= 32) ? warp_sums[(threadIdx.x >> 5) - 1] : 0u);
+    for (unsigned i = lo; i < hi; ++i) {
+        const unsigned v = in[i];
+        out[i] = run;
+        run += v;
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        const unsigned t = warp_sums[31];
+        out[n] = t;
+        *total = t;
     }
 }
 
@@ -320,12 +344,13 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(MapDev m, unsigne
                                                                float *points, float *normals, int *cases,
                                                                int *cube_xyz) {
     __shared__ float s[kN3];
-    __shared__ signed char tri[256][kMcMaxTriIdx];
-    __shared__ unsigned char count[256];
+    __shared__ __align__(16) signed char tri[256][kMcMaxTriIdx];
+    __shared__ __align__(16) unsigned char count[256];
     __shared__ unsigned short slot[kMaxBlockTris];  // output slot -> cube << 4 | triangle of the cube
     __shared__ unsigned char ucase[kBlockVoxels];  // case index of each cube with triangles
     __shared__ unsigned wsum[kEmitThreads / 32];
-    for (int i = threadIdx.x; i < 256 * kMcMaxTriIdx; i += blockDim.x) (&tri[0][0])[i] = (&c_tri_table[0][0])[i];
+    for (int i = threadIdx.x; i < 256 * kMcMaxTriIdx / 16; i += blockDim.x)
+        reinterpret_cast<int4 *>(&tri[0][0])[i] = reinterpret_cast<const int4 *>(g_mc_tri)[i];
     load_counts(count);
     const float vs = m.voxel_size;
     for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
