@@ -6,7 +6,7 @@ depth noise, 1 % dropout), 5 mm voxels, truncation 3 voxels, 2^21 hash
 slots, FP16 TSDF + u8 weight (rounding residual kept), 3-level RGB+ICP pyramid with {10,5,3} GN
 iterations.  A step is one frame of the sequence through the whole dense
 path: image and depth pyramids, raycast of the map at the previous pose,
-model pyramid, 18 Gauss-Newton iterations with the device-side FP64 solve,
+model pyramid, 18 Gauss-Newton iterations with the device-side double-float solve,
 frame-step check, pose update, block allocation, visibility, integration.
 
 value: frames/s with the frame already in HBM (one device-to-device copy
@@ -312,7 +312,7 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 compute, fp16 TSDF storage, fp64 solve",
+        "dtype": "fp32 compute, fp16 TSDF storage, double-float (fp32-pair) solve",
         "data": "synthetic (seeded analytic RGB-D scene; no dataset)",
         "config": dict(WORKLOAD),
         "storage": GPU_STORAGE,
@@ -744,7 +744,7 @@ def cpu_baseline(frames, K, nmax: int, budget_s: float = 20.0, check_frames: int
 
 
 def precision_check(frames, K):
-    """The benchmarked form (FP16 TSDF words, compensated sums, FP64 solve)
+    """The benchmarked form (FP16 TSDF words, compensated sums, double-float solve)
     against the FP64 oracle on a prefix of the benchmark's sequence:
     - tracking, closed loop: the session's pose and each frame's motion
       estimate against the oracle session's (metres / radians);
@@ -802,7 +802,7 @@ def precision_check(frames, K):
         return {"max": float(x.max()), "p99": float(np.percentile(x, 99)), "p50": float(np.median(x))}
 
     return {"against": "the oracle's FP64 build (checker), same frames",
-            "form": GPU_STORAGE + ", compensated FP32 sums, FP64 solve",
+            "form": GPU_STORAGE + ", compensated FP32 sums, double-float solve",
             "frames": len(frames),
             "pose_m": st(pose_t), "pose_rad": st(pose_r),
             "frame_motion_m": st(step_t), "frame_motion_rad": st(step_r),

@@ -253,11 +253,12 @@ YAS_API int yas_tracker_get_transform(yas_tracker *tr, const yas_pose *init, int
  * rounding of a different summation order. */
 YAS_API int yas_tracker_set_schedule(yas_tracker *tr, int fused);
 /* How the Gauss-Newton sums are totalled across the GPU.  1 (default):
- * compensated FP32 (TwoSum) partial sums with FP64 totals.  0: plain FP32
- * sums in the same order, the reference's arithmetic (WarpReduceSum /
- * BlockReduceSum and cv::cuda::reduce in FP32, TrackingUtils.h:8-58,
- * RGBDTracking.cu:253-286), for precision comparisons.  The solve is FP64
- * either way.  Takes effect at the next GetTransform, captured graphs
+ * compensated FP32 (TwoSum) partial sums, totals kept as double-float pairs
+ * (FP64 totals in the per-iteration passes).  0: plain FP32 sums in the same
+ * order, the reference's arithmetic (WarpReduceSum / BlockReduceSum and
+ * cv::cuda::reduce in FP32, TrackingUtils.h:8-58, RGBDTracking.cu:253-286),
+ * for precision comparisons.  The solve is double-float (48 significant
+ * bits) either way.  Takes effect at the next GetTransform, captured graphs
  * included. */
 YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated);
 /* Checks the fused GN schedule's bounded waits (no counterpart in the
@@ -268,12 +269,14 @@ YAS_API int yas_tracker_set_reduction(yas_tracker *tr, int compensated);
  * when the limit works).  The tracker stays usable; its next GetTransform
  * starts from a reset state.  Takes about one second. */
 YAS_API int yas_tracker_check_wait_limit(yas_tracker *tr, int *out_status);
-/* Checks the FP64 division the device solve uses for its pivots (no
- * counterpart in the reference: the reference divides on the host in Eigen).
- * out[i] = a[i] / x[i] computed on the device as the solve computes it:
- * Newton-Raphson refinement (one step) of an FP32 reciprocal seed for
- * 1e-30 < |x| < 1e30, IEEE division outside that range.  Host arrays of n
- * doubles, 0 < n <= 1 << 20; waits for the result. */
+/* Checks the division the device solve uses for its pivots (no counterpart
+ * in the reference: the reference divides on the host in Eigen).
+ * out[i] = a[i] / x[i] computed on the device as the solve computes it: the
+ * operands rounded to double-float (FP32 pairs), the FP32 reciprocal of the
+ * divisor's high part refined by one Newton-Raphson step and multiplied by
+ * the dividend, for 1e-30 < |x| < 1e30; an FP64 division of the rounded
+ * operands outside that range.  Host arrays of n doubles, 0 < n <= 1 << 20;
+ * waits for the result. */
 YAS_API int yas_check_div_seeded(const double *a, const double *x, double *out, int n);
 /* SwapFrameBuffer / IsTrackingGood: RGBDTracking.h:28,15 / RGBDTracking.cu:294-303,551-554. */
 YAS_API int yas_tracker_swap_frame_buffer(yas_tracker *tr);

@@ -10,9 +10,9 @@ sessions run the same frames:
   f32_plain  FP32 TSDF,                            plain FP32 sums
   f16_plain  FP16 TSDF,                            plain FP32 sums
 
-(compensated = TwoSum partial sums with FP64 totals; plain = the same order
-without error terms, the reference's arithmetic; the 6x6 solve and the SE(3)
-update are FP64 in all four).  The oracle (FP64 restatement of the
+(compensated = TwoSum partial sums with double-float totals; plain = the
+same order without error terms, the reference's arithmetic; the 6x6 solve
+and the SE(3) update are double-float, 48 significant bits, in all four).  The oracle (FP64 restatement of the
 reference's integrate / raycast / mesh / tracking math) runs the same frames.
 Reported:
 

@@ -201,27 +201,26 @@ def test_bounded_wait_reports_timeout_and_tracker_recovers(cuda, mode):
 
 
 def test_seeded_division_against_ieee(native, cuda):
-    """The solve's pivot division (Newton-Raphson refinement of an FP32
-    reciprocal seed, gn_solve.cuh: div_seeded) against IEEE division: relative
-    error below 2^-43 over the seed range 1e-30 < |x| < 1e30 (the method's bound
-    is 2^-44 plus FP64 roundings), and exactly IEEE outside it."""
-    import ctypes as C
-
+    """The solve's pivot division (gn_solve.cuh: df_div, double-float: the FP32
+    reciprocal of the divisor's high part refined by one Newton-Raphson step,
+    times the dividend) against IEEE FP64 division of the same operands:
+    relative error below 2^-43 (each operand is first rounded to double-float,
+    2^-49; the refined reciprocal is within 2^-44; the product adds 2^-47).
+    Divisors span 1e-29 < |x| < 1e36: the seed range 1e-30 < |x| < 1e30 and,
+    above it, the FP64 division of the rounded operands; quotients stay above
+    1e-30, where the low part of a double-float is a normal FP32 number."""
     rng = np.random.default_rng(5)
     n = 1 << 18
-    x = np.exp(rng.uniform(np.log(1e-29), np.log(1e29), n)) * rng.choice([-1.0, 1.0], n)
+    x = np.exp(rng.uniform(np.log(1e-29), np.log(1e36), n)) * rng.choice([-1.0, 1.0], n)
     a = np.exp(rng.uniform(np.log(1e-6), np.log(1e6), n)) * rng.choice([-1.0, 1.0], n)
     x[:16] = [1.0, -1.0, 2.0, 3.0, 1e-29, -1e29, 0.1, 1.0 / 3.0, np.nextafter(1.0, 2.0), 7.0, 1e20, 1e-20, 5e28,
-              6e-29, 0.5, 1.5]
+              6e-29, 2e30, -3e35]
+    # quotients inside the normal FP32 range with room for the low part
+    a = np.where(np.abs(a / x) < 1e-28, a * 1e12, a)
     out = np.zeros(n)
     L = native
     assert L.yas_check_div_seeded(a.ctypes.data, x.ctypes.data, out.ctypes.data, n) == 0
     rel = np.abs(out - a / x) / np.abs(a / x)
     assert rel.max() <= 2.0 ** -43, rel.max()
-    # outside the seed range: IEEE division, bit for bit
-    xo = np.array([1e-31, -1e-40, 2e30, -1e300, 0.0, np.inf, 1e-310])
-    ao = np.ones_like(xo) * 3.0
-    oo = np.zeros_like(xo)
-    assert L.yas_check_div_seeded(ao.ctypes.data, xo.ctypes.data, oo.ctypes.data, xo.size) == 0
-    with np.errstate(divide="ignore", over="ignore"):
-        assert np.array_equal(oo, ao / xo)
+    inside = (np.abs(x) > 1e-30) & (np.abs(x) < 1e30)
+    print(f"df_div: max relative error {rel[inside].max():.3g} in the seed range, {rel[~inside].max():.3g} above it")

@@ -355,17 +355,23 @@ __device__ __forceinline__ float bilinear(const float *__restrict__ m, int w, fl
 }
 
 // Huber threshold 4.685 * stddev of the photometric residuals, in FP32 as the
-// reference (RGBDTracking.cu:259-278), from the FP64 totals n = tot[29],
-// sum r = tot[30], sum r^2 = tot[31]: mean = sum r / n, then
+// reference (RGBDTracking.cu:259-278), from the double-float totals
+// n = tot[29], sum r = tot[30], sum r^2 = tot[31]: mean = sum r / n, then
 // sum (r - mean)^2 = sum r^2 - 2 mean sum r + n mean^2 (the reference's second
 // pass over the residuals).
-__device__ __forceinline__ float huber_threshold(const double *tot) {
-    const double nn = tot[29], s = tot[30], s2 = tot[31];
-    const float mean = (float)s / (float)nn;
-    const double md = (double)mean;
-    const double ss = fma(nn * md, md, fma(-2.0 * md, s, s2));
-    const float var = sqrtf((float)ss / ((float)nn - 1.0f));
+__device__ __forceinline__ float huber_threshold_df(DF nn, DF s, DF s2) {
+    // nn.h, s.h: the totals rounded to FP32 (normalised pairs)
+    const float mean = s.h / nn.h;
+    const DF md = df(mean);
+    const DF ss = df_fma(df_mul(nn, md), md, df_fma(df(-2.0f * mean), s, s2));
+    const float var = sqrtf(ss.h / (nn.h - 1.0f));
     return (float)(4.685 * (double)var);
+}
+__device__ __forceinline__ float huber_threshold(const double *tot) {
+    return huber_threshold_df(df_from_double(tot[29]), df_from_double(tot[30]), df_from_double(tot[31]));
+}
+__device__ __forceinline__ float huber_threshold_solve() {
+    return huber_threshold_df(total(0, 29), total(0, 30), total(0, 31));
 }
 
 __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
@@ -421,7 +427,7 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_a(PassArgs a) {
     if (threadIdx.x == 0) st->huber_th = huber_threshold(tot);
     if (a.mode == YAS_TRACK_ICP) {
         load_solve_state(st);
-        if (threadIdx.x < 32) g_solve.A[threadIdx.x] = tot[threadIdx.x];
+        if (threadIdx.x < 32) set_total_double(0, threadIdx.x, tot[threadIdx.x]);
         if (threadIdx.x == 0) g_solve.huber_th = huber_threshold(tot);
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -474,8 +480,8 @@ __global__ void __launch_bounds__(kTrackThreads, 4) gn_pass_b(PassArgs a) {
     load_solve_state(st);
     if (threadIdx.x < 32) {
         st->b_sums[threadIdx.x] = tot[threadIdx.x];
-        g_solve.B[threadIdx.x] = tot[threadIdx.x];
-        g_solve.A[threadIdx.x] = __ldcg(&st->a_sums[threadIdx.x]);
+        set_total_double(1, threadIdx.x, tot[threadIdx.x]);
+        set_total_double(0, threadIdx.x, __ldcg(&st->a_sums[threadIdx.x]));
     }
     if (threadIdx.x == 0) g_solve.huber_th = th;
     __syncthreads();
@@ -516,7 +522,7 @@ __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) 
 //      [RGB] fold of the three photometric moments -> Huber threshold;
 //   2. [RGB] pass B (weighted photometric products, from the residuals each
 //      thread kept in registers) -> row B;
-//   3. fold of the ICP and photometric systems -> FP64 solve -> estimate.
+//   3. fold of the ICP and photometric systems -> solve -> estimate.
 // Rows are double-buffered by iteration parity: a CTA can run at most one
 // iteration ahead of the slowest reader of a buffer.  Every wait is bounded by
 // a wall-clock limit: a CTA that gives up raises the state's abort word, every
@@ -665,8 +671,9 @@ __device__ __forceinline__ void fused_publish_row(float v[32], unsigned long lon
 }
 
 // Totals over all CTAs of the photometric moments (columns 29..31 of rows A)
-// into g_solve.A[29..31]; compensated FP32 per column (32 lanes x 5 rows,
-// then a butterfly), FP64 at the end.  False on abort or timeout.
+// into the solve's totals 29..31 of pass A; compensated FP32 per column (32
+// lanes x 5 rows, then a butterfly), kept as a double-float pair.  False on
+// abort or timeout.
 __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, unsigned nrows, unsigned tag,
                                              GNState *st, bool plain) {
     __shared__ float m3[3][kFusedMaxCtas];
@@ -706,18 +713,18 @@ __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, uns
             h = s;
             l = (l + ol) + e;
         }
-        if (lane == 0) g_solve.A[29 + warp] = plain ? (double)h : (double)h + (double)l;
+        if (lane == 0) set_total(0, 29 + warp, h, plain ? 0.0f : l);
     }
     __syncthreads();
     return true;
 }
 
-// Totals over all CTAs of the ICP system (columns 0..28 of rows A) into
-// g_solve.A[0..28] and of the photometric system (columns 0..27 of rows B)
-// into g_solve.B[0..27] (zero for a term the mode does not use).  Thread t
-// folds column t % 64 over the rows of subset t / 64 (compensated FP32), then
-// a butterfly over the 16 subsets of each column; FP64 at the end.  False on
-// abort or timeout.
+// Totals over all CTAs of the ICP system (columns 0..28 of rows A) into the
+// solve's pass A totals 0..28 and of the photometric system (columns 0..27 of
+// rows B) into its pass B totals 0..27 (zero for a term the mode does not
+// use).  Thread t folds column t % 64 over the rows of subset t / 64
+// (compensated FP32), then a butterfly over the 16 subsets of each column;
+// each total is kept as a double-float pair.  False on abort or timeout.
 __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, const unsigned long long *rowsB,
                                              unsigned nrows, unsigned tag, bool icp, bool rgb, GNState *st,
                                              bool plain) {
@@ -773,9 +780,8 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
             l2 = (l2 + ol) + e;
         }
         if (s_ == 0) {
-            const double v = plain ? (double)h2 : (double)h2 + (double)l2;
-            if (col < 29) g_solve.A[col] = v;
-            else if (col >= 32 && col < 60) g_solve.B[col - 32] = v;
+            if (col < 29) set_total(0, col, h2, plain ? 0.0f : l2);
+            else if (col >= 32 && col < 60) set_total(1, col - 32, h2, plain ? 0.0f : l2);
         }
     }
     __syncthreads();
@@ -797,8 +803,10 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
     const bool do_rgb = (mode & YAS_TRACK_RGB) != 0, do_icp = (mode & YAS_TRACK_ICP) != 0;
     load_solve_state(st);
     if (t >= 32 && t < 64) {
-        g_solve.A[t - 32] = 0.0;
-        g_solve.B[t - 32] = 0.0;
+        g_solve.Ah[t - 32] = 0.0f;
+        g_solve.Al[t - 32] = 0.0f;
+        g_solve.Bh[t - 32] = 0.0f;
+        g_solve.Bl[t - 32] = 0.0f;
     }
     const unsigned epoch = __ldcg(&st->epoch);
     const bool plain = __ldcg(&st->plain_sums) != 0u;
@@ -845,7 +853,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             fused_publish_row(acc, rA + cta * 32, tag);
             if (do_rgb) {
                 if (!fold_moments(rA, nrows, tag, st, plain)) return;
-                if (t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
+                if (t == 0) g_solve.huber_th = huber_threshold_solve();
                 __syncthreads();
                 const float th = g_solve.huber_th;
 #pragma unroll
@@ -871,7 +879,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             }
             if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st, plain)) return;
             if (t < 32) {
-                if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold(g_solve.A);
+                if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold_solve();
                 gn_solve(mode, 0, it == 0, l);
             }
             __syncthreads();
@@ -883,8 +891,8 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
     }
     if (cta == 0 && t < 32) {
         publish_solve(st);
-        st->a_sums[t] = g_solve.A[t];
-        st->b_sums[t] = g_solve.B[t];
+        st->a_sums[t] = df_to_double(total(0, t));
+        st->b_sums[t] = df_to_double(total(1, t));
     }
 }
 
@@ -1415,11 +1423,11 @@ extern "C" YAS_API int yas_gn_linearise_static(const yas_gn_level *lv, const yas
     return YAS_OK;
 }
 
-// ---------------------------------------------------------------- self-check of the seeded division
+// ---------------------------------------------------------------- self-check of the solve's division
 namespace yas {
-__global__ void div_seeded_kernel(const double *a, const double *x, double *out, int n) {
+__global__ void df_div_kernel(const double *a, const double *x, double *out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = div_seeded(a[i], x[i]);
+    if (i < n) out[i] = df_to_double(df_div(df_from_double(a[i]), df_from_double(x[i])));
 }
 }  // namespace yas
 
@@ -1432,7 +1440,7 @@ extern "C" YAS_API int yas_check_div_seeded(const double *a, const double *x, do
     cudaError_t e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d + n, x, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        div_seeded_kernel<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, n);
+        df_div_kernel<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);

@@ -46,7 +46,7 @@ struct __align__(16) GNState {
     double last_update[6];
     unsigned epoch;         // launches of the fused schedule (row tags)
     unsigned abort_word;    // set when a bounded wait of the fused schedule gave up
-    unsigned plain_sums;    // 1: plain FP32 totals (the reference's); 0: compensated, FP64 totals
+    unsigned plain_sums;    // 1: plain FP32 totals (the reference's); 0: compensated totals
 };
 
 // One pyramid level of a fused Gauss-Newton schedule: camera, iterations,

@@ -360,7 +360,7 @@ class RGBDTracking:
         L.call("yas_tracker_set_schedule", self.handle, int(fused))
 
     def set_reduction(self, compensated: bool) -> None:
-        """Compensated FP32 sums with FP64 totals (True) or plain FP32 sums (False)."""
+        """Compensated FP32 sums with double-float totals (True) or plain FP32 sums (False)."""
         L.call("yas_tracker_set_reduction", self.handle, int(compensated))
 
     def check_wait_limit(self) -> int:
