@@ -272,9 +272,9 @@ YAS_API int yas_tracker_check_wait_limit(yas_tracker *tr, int *out_status);
 /* Checks the division the device solve uses for its pivots (no counterpart
  * in the reference: the reference divides on the host in Eigen).
  * out[i] = a[i] / x[i] computed on the device as the solve computes it: the
- * operands rounded to double-float (FP32 pairs), the FP32 reciprocal of the
- * divisor's high part refined by one Newton-Raphson step and multiplied by
- * the dividend, for 1e-30 < |x| < 1e30; an FP64 division of the rounded
+ * operands rounded to double-float (FP32 pairs), the approximate FP32
+ * reciprocal of the divisor's high part refined by one Newton-Raphson step
+ * and multiplied by the dividend, for 1e-30 < |x| < 1e30; an FP64 division of the rounded
  * operands outside that range.  Host arrays of n doubles, 0 < n <= 1 << 20;
  * waits for the result. */
 YAS_API int yas_check_div_seeded(const double *a, const double *x, double *out, int n);

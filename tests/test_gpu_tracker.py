@@ -201,11 +201,12 @@ def test_bounded_wait_reports_timeout_and_tracker_recovers(cuda, mode):
 
 
 def test_seeded_division_against_ieee(native, cuda):
-    """The solve's pivot division (gn_solve.cuh: df_div, double-float: the FP32
-    reciprocal of the divisor's high part refined by one Newton-Raphson step,
-    times the dividend) against IEEE FP64 division of the same operands:
-    relative error below 2^-43 (each operand is first rounded to double-float,
-    2^-49; the refined reciprocal is within 2^-44; the product adds 2^-47).
+    """The solve's pivot division (gn_solve.cuh: df_div, double-float: the
+    approximate FP32 reciprocal of the divisor's high part refined by one
+    Newton-Raphson step, times the dividend) against IEEE FP64 division of the
+    same operands: relative error below 2^-43 (each operand is first rounded to
+    double-float, 2^-49; the refined reciprocal is within 2^-44 (the square of
+    the seed's 2^-22) plus its roundings; the product adds 2^-47).
     Divisors span 1e-29 < |x| < 1e36: the seed range 1e-30 < |x| < 1e30 and,
     above it, the FP64 division of the rounded operands; quotients stay above
     1e-30, where the low part of a double-float is a normal FP32 number."""

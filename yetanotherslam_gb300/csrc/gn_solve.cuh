@@ -38,9 +38,9 @@
 // trailing matrix and b at once; pivot and NaN tests are integer bit
 // operations on the high parts; the SE(3) exponential computes its three
 // series on three lanes and one entry of [R | t] per lane.  An elimination
-// step divides through the pivot's reciprocal: the FP32 reciprocal of the
-// high part refined by one Newton-Raphson step in double-float, formed while
-// the products a_ik a_jk are.
+// step divides through the pivot's reciprocal: the approximate FP32
+// reciprocal of the high part refined by one Newton-Raphson step in
+// double-float, formed while the products a_ik a_jk are.
 #pragma once
 
 #include <cfloat>
@@ -112,13 +112,19 @@ __device__ __forceinline__ bool df_seed_range(DF x) {
     return a > 0x0da24260u && a < 0x7149f2cau;
 }
 
-// 1 / d: r0 = FP32 reciprocal of d.h, e = 1 - d r0 (1 - fl(d.h r0) is exact:
-// Sterbenz), r = r0 + r0 e.  Relative error below 2^-44 in the seed range;
-// outside it an FP64 division (pivots of a Gauss-Newton system stay far
-// inside: its entries are sums of squared image and depth gradients).
+// 1 / d: r0 = the hardware's approximate FP32 reciprocal of d.h (relative
+// error below 2^-22), e = 1 - d r0 (1 - fl(d.h r0) is exact: Sterbenz),
+// r = r0 + r0 e, one Newton-Raphson step.  Relative error below 2^-43 in the
+// seed range; outside it an FP64 division (pivots of a Gauss-Newton system
+// stay far inside: its entries are sums of squared image and depth gradients).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ DF df_rcp(DF d) {
     if (!df_seed_range(d)) return df_from_double(1.0 / df_to_double(d));
-    const float r0 = __frcp_rn(d.h);
+    const float r0 = rcp_approx(d.h);
     const float p = __fmul_rn(d.h, r0);
     const float pe = __fmaf_rn(d.h, r0, -p);
     const float e = __fmaf_rn(-d.l, r0, __fsub_rn(__fsub_rn(1.0f, p), pe));
@@ -257,20 +263,36 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
             for (int r = 0; r < 6; ++r) rq += (kd[r] > kd[q] || (kd[r] == kd[q] && r < q)) ? 1 : 0;
             pos[q] = rq;
         }
+        // inverse permutation, the largest key and this lane's pivot rows by
+        // selects (registers, no indexed local arrays)
         int inv[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) inv[pos[q]] = q;
+        for (int p = 0; p < 6; ++p) {
+            int v = 0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) v = pos[q] == p ? q : v;
+            inv[p] = v;
+        }
+        int kmax = kd[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q) kmax = max(kmax, kd[q]);
         // no factorisation when the largest diagonal is zero or the first is NaN
-        const int kmax = kd[inv[0]];
         broke = kmax <= 0 || kd[0] == -1;
         if (!broke) {
-            const int pi = ism || isb ? inv[ei] : 0;
-            const int pj = ism ? inv[ej] : 0;
+            int pi = 0, pj = 0;
+#pragma unroll
+            for (int p = 0; p < 6; ++p) {
+                pi = ei == p ? inv[p] : pi;
+                pj = ej == p ? inv[p] : pj;
+            }
+            pi = ism || isb ? pi : 0;
+            pj = ism ? pj : 0;
             const int src = ism ? (pi >= pj ? tri_lane(pi, pj) : tri_lane(pj, pi)) : (isb ? 21 + pi : lane);
             a = df_shfl(a, src);
             if (isb) orig = pi;
         }
     }
+    DF rk = df(0.0f);  // b lane i: reciprocal of pivot i (for D^+ y)
     if (!broke) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -290,6 +312,7 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
             const DF nl = df_mul(a, r);
             if (upd && (isb || valid)) a = na;
             if (colk) a = nl;
+            if (isb && ei == k) rk = r;
         }
     }
     if (broke) {  // forward substitution with the unfactored lower triangle
@@ -302,10 +325,12 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
             if (u) a = na;
         }
     }
-    {  // D^+ y on the b lanes (a zero or NaN pivot gives 0; an infinite one 0)
+    {  // D^+ y on the b lanes (a zero or NaN pivot gives 0; an infinite one 0):
+       // times the pivot's reciprocal from the factorisation (the diagonal is
+       // final once its step has run), a division when nothing was factorised
         const DF dd = df_shfl(a, isb ? tri_lane(ei, ei) : lane);
         const unsigned db = __float_as_uint(dd.h) & kAbsMaskF;
-        if (isb) a = (db != 0u && db < kInfBitsF) ? df_div(a, dd) : df(0.0f);
+        if (isb) a = (db != 0u && db < kInfBitsF) ? (broke ? df_div(a, dd) : df_mul(a, rk)) : df(0.0f);
     }
     // ---- L^T z = y: b_i -= L(j, i) z_j for j > i
 #pragma unroll
