@@ -511,7 +511,7 @@ __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) 
 
 // ---------------------------------------------------------------- fused schedule
 // One cooperative launch runs every Gauss-Newton iteration of every level
-// (GetTransform's loops, RGBDTracking.cu:161-208), one 1024-thread CTA per SM,
+// (GetTransform's loops, RGBDTracking.cu:161-208), one 512-thread CTA per SM,
 // CTA c owning the pixel range [c * chunk, (c + 1) * chunk) of each level.
 // Nothing is released by one CTA to the others: each CTA publishes its row
 // of partial sums as tagged 64-bit words {value, tag} (tag = launch epoch and
@@ -528,11 +528,25 @@ __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) 
 // a wall-clock limit: a CTA that gives up raises the state's abort word, every
 // waiter leaves as soon as it sees it, and the state reports kFailTimeout.
 // CTA 0 writes the final state to global memory.
-constexpr int kFusedThreads = 1024;
-constexpr int kFusedWarps = kFusedThreads / 32;
-constexpr int kFoldSubsets = 16;    // row subsets of the system fold
-constexpr int kFoldRows = 10;       // rows per subset
-constexpr int kFusedMaxCtas = kFoldSubsets * kFoldRows;  // 160
+// CTA size NT: 512 threads when every thread keeps its pixels' residuals in
+// registers (PIX = 1, 2, 4), 1024 otherwise (PIX = 0, and the batched
+// schedules, whose CTAs own many pixels each and are latency-bound on them).
+// A row costs each warp a 31-shuffle transpose reduction (shuffles issue at
+// one warp instruction per cycle per SM), so 512 threads halve that
+// twice-per-iteration cost, and 128 registers per thread hold four level-0
+// pixels' residuals without spills (measured at 640x480: 244 against 252 us
+// per launch; the batched and the PIX = 0 schedules were slower at 512).
+constexpr int kFusedMaxCtas = 160;  // rows the system fold covers
+template <int PIX>
+constexpr int fused_threads() { return PIX == 0 ? 1024 : 512; }
+constexpr int kBatchThreads = 1024;
+template <int NT>
+struct FoldShape {
+    static constexpr int warps = NT / 32;
+    static constexpr int subsets = NT / 64;                 // row subsets of the system fold
+    static constexpr int rows = kFusedMaxCtas / subsets;    // rows per subset
+    static_assert(subsets * rows == kFusedMaxCtas && 3 * kFusedMaxCtas <= NT, "fold shape");
+};
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
 
 
@@ -652,7 +666,9 @@ __device__ __forceinline__ void fused_pixel_b(const LevelCam &c, float th, const
 
 // The CTA's row of 32 sums (warp transpose sums, then a pairwise tree over
 // the 32 warp sums of each value), published by warp 0 as tagged words.
+template <int NT>
 __device__ __forceinline__ void fused_publish_row(float v[32], unsigned long long *row, unsigned tag) {
+    constexpr int kFusedWarps = FoldShape<NT>::warps;
     __shared__ float wsum[kFusedWarps][33];
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const float r = warp_transpose_reduce(v);
@@ -723,11 +739,14 @@ __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, uns
 // solve's pass A totals 0..28 and of the photometric system (columns 0..27 of
 // rows B) into its pass B totals 0..27 (zero for a term the mode does not
 // use).  Thread t folds column t % 64 over the rows of subset t / 64
-// (compensated FP32), then a butterfly over the 16 subsets of each column;
+// (compensated FP32), then a butterfly over the 8 subsets of each column;
 // each total is kept as a double-float pair.  False on abort or timeout.
+template <int NT>
 __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, const unsigned long long *rowsB,
                                              unsigned nrows, unsigned tag, bool icp, bool rgb, GNState *st,
                                              bool plain) {
+    constexpr int kFoldSubsets = FoldShape<NT>::subsets, kFoldRows = FoldShape<NT>::rows;
+    constexpr int kFusedWarps = FoldShape<NT>::warps;
     __shared__ float hs[kFoldSubsets][65], ls[kFoldSubsets][65];
     const int t = (int)threadIdx.x, c = t & 63, sub = t >> 6;
     const bool need = (c < 29 && icp) || (c >= 32 && c < 60 && rgb);
@@ -767,12 +786,13 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
     hs[sub][c] = h;
     ls[sub][c] = l;
     if (!__syncthreads_and(mine)) return false;
-    {  // warp w folds columns 2w and 2w + 1, lanes 0..15 / 16..31 = subsets
+    {  // warp w folds columns n w + c (n = 64 / warps), lanes c S .. c S + S - 1 = the S subsets
+        constexpr int kColsPerWarp = 64 / kFusedWarps;
         const int warp = t >> 5, lane = t & 31;
-        const int col = 2 * warp + (lane >> 4), s_ = lane & 15;
+        const int col = kColsPerWarp * warp + lane / kFoldSubsets, s_ = lane % kFoldSubsets;
         float h2 = hs[s_][col], l2 = ls[s_][col];
 #pragma unroll
-        for (int off = 8; off >= 1; off >>= 1) {
+        for (int off = kFoldSubsets / 2; off >= 1; off >>= 1) {
             const float oh = __shfl_xor_sync(0xffffffffu, h2, off), ol = __shfl_xor_sync(0xffffffffu, l2, off);
             float s, e;
             two_sum(h2, oh, s, e);
@@ -790,11 +810,11 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
 
 // The fused schedule of one tracker, run by `nrows` CTAs (this one is `cta`).
 // Level l's pixel k = cta * chunk_l + off, off < chunk_l.  PIX > 0: a thread
-// owns at most PIX pixels per level (off = s * kFusedThreads + thread) and
+// owns at most PIX pixels per level (off = s * NT + thread, NT threads) and
 // keeps their residuals in registers for pass B; PIX == 0: any number of
 // pixels, residuals through `res4` (pass B then recomputes the warped point,
 // as gn_pass_b does).
-template <int PIX>
+template <int PIX, int NT>
 __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mode, float angle_th, float dist_th,
                                             unsigned long long *rows, float4 *res4, GNState *st, unsigned cta,
                                             unsigned nrows) {
@@ -834,14 +854,14 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                 for (int q = 0; q < PIX; ++q) {
                     res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
                     pp[q] = make_float3(0.0f, 0.0f, 1.0f);
-                    const int off = q * kFusedThreads + t;
+                    const int off = q * NT + t;
                     const int k = base + off;
                     if (q < lv.pix && off < lv.chunk && k < n)
                         fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, res[q], pp[q]);
                 }
             } else {
 #pragma unroll 2
-                for (int off = t; off < lv.chunk; off += kFusedThreads) {
+                for (int off = t; off < lv.chunk; off += NT) {
                     const int k = base + off;
                     if (k >= n) break;
                     float4 r4;
@@ -850,7 +870,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     if (do_rgb) res4[k] = r4;
                 }
             }
-            fused_publish_row(acc, rA + cta * 32, tag);
+            fused_publish_row<NT>(acc, rA + cta * 32, tag);
             if (do_rgb) {
                 if (!fold_moments(rA, nrows, tag, st, plain)) return;
                 if (t == 0) g_solve.huber_th = huber_threshold_solve();
@@ -864,7 +884,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                         if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
                 } else {
 #pragma unroll 2
-                    for (int off = t; off < lv.chunk; off += kFusedThreads) {
+                    for (int off = t; off < lv.chunk; off += NT) {
                         const int k = base + off;
                         if (k >= n) break;
                         const float4 r4 = res4[k];
@@ -875,9 +895,9 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                         }
                     }
                 }
-                fused_publish_row(acc, rB + cta * 32, tag);
+                fused_publish_row<NT>(acc, rB + cta * 32, tag);
             }
-            if (!fold_systems(rA, rB, nrows, tag, do_icp, do_rgb, st, plain)) return;
+            if (!fold_systems<NT>(rA, rB, nrows, tag, do_icp, do_rgb, st, plain)) return;
             if (t < 32) {
                 if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold_solve();
                 gn_solve(mode, 0, it == 0, l);
@@ -898,8 +918,8 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
 
 // The fused schedule of one tracker over the whole grid.
 template <int PIX>
-__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_constant__ FusedArgs a) {
-    gn_schedule<PIX>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, a.res4, a.st, blockIdx.x, gridDim.x);
+__global__ void __launch_bounds__(fused_threads<PIX>(), 1) gn_fused(const __grid_constant__ FusedArgs a) {
+    gn_schedule<PIX, fused_threads<PIX>()>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, a.res4, a.st, blockIdx.x, gridDim.x);
 }
 
 // Fused schedules of a batch of trackers in one launch: CTA b runs for item
@@ -908,11 +928,11 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gn_fused(const __grid_consta
 // PIX > 0: every item's CTAs own at most PIX pixels per thread on every level
 // (residuals kept in registers); PIX == 0: any share (residuals in res4).
 template <int PIX>
-__global__ void __launch_bounds__(kFusedThreads, 1) gn_fused_batch(const GNBatchItem *__restrict__ items,
+__global__ void __launch_bounds__(kBatchThreads, 1) gn_fused_batch(const GNBatchItem *__restrict__ items,
                                                                     const unsigned short *__restrict__ cta_item) {
     const GNBatchItem &it = items[cta_item[blockIdx.x]];
-    gn_schedule<PIX>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st,
-                     blockIdx.x - (unsigned)it.cta0, (unsigned)it.nctas);
+    gn_schedule<PIX, kBatchThreads>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st,
+                                    blockIdx.x - (unsigned)it.cta0, (unsigned)it.nctas);
 }
 
 // ---------------------------------------------------------------- host side
@@ -981,7 +1001,7 @@ template <int PIX>
 static cudaError_t launch_fused_pix(const FusedArgs &a, int grid, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kFusedThreads);
+    cfg.blockDim = dim3(fused_threads<PIX>());
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -992,7 +1012,7 @@ static cudaError_t launch_fused_pix(const FusedArgs &a, int grid, cudaStream_t s
     return cudaLaunchKernelEx(&cfg, gn_fused<PIX>, a);
 }
 
-// Grid of the fused schedule: every co-resident 1024-thread CTA (one per SM),
+// Grid of the fused schedule: one CTA per SM (512 threads; 1024 for PIX = 0),
 // at most kFusedMaxCtas (the rows the system fold covers).  Level l gives each CTA a
 // chunk of ceil(P_l / grid) pixels rounded up to a warp; `pix` is the smallest
 // compiled pixels-per-thread bound (1, 2 or 4) that covers level 0's chunk,
@@ -1005,12 +1025,14 @@ static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         int nb[4] = {0, 0, 0, 0};
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], gn_fused<1>, kFusedThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], gn_fused<2>, kFusedThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], gn_fused<4>, kFusedThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[3], gn_fused<0>, kFusedThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], gn_fused<1>, fused_threads<1>(), 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], gn_fused<2>, fused_threads<2>(), 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], gn_fused<4>, fused_threads<4>(), 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[3], gn_fused<0>, fused_threads<0>(), 0);
         cudaGetLastError();
-        for (int i = 0; i < 4; ++i) tr->fused_max_grid[i] = coop ? std::min(nb[i] * sms, kFusedMaxCtas) : 0;
+        // one CTA per SM (the schedule's design), whatever else would fit
+        for (int i = 0; i < 4; ++i)
+            tr->fused_max_grid[i] = coop ? std::min(std::min(nb[i], 1) * sms, kFusedMaxCtas) : 0;
     }
     const long long P0 = (long long)tr->cam[0].w * tr->cam[0].h;
     const int pixes[3] = {1, 2, 4};
@@ -1018,7 +1040,7 @@ static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
         const int g = tr->fused_max_grid[i];
         if (g <= 0) continue;
         const long long chunk = ((P0 + g - 1) / g + 31) / 32 * 32;
-        if (chunk <= (long long)kFusedThreads * pixes[i]) {
+        if (chunk <= (long long)fused_threads<1>() * pixes[i]) {
             pix = pixes[i];
             grid = g;
             return true;
@@ -1034,14 +1056,14 @@ static bool fused_plan(yas_tracker *tr, int &pix, int &grid) {
 }
 
 // Levels of a fused schedule run by `grid` CTAs, on the tracker's current sets.
-static void fill_levels(yas_tracker *tr, int grid, FusedLevel *lv) {
+static void fill_levels(yas_tracker *tr, int grid, int threads, FusedLevel *lv) {
     for (int l = 0; l < tr->L; ++l) {
         FusedLevel &f = lv[l];
         f.c = tr->cam[l];
         f.iters = tr->iters[l];
         const long long P = (long long)f.c.w * f.c.h;
         f.chunk = (int)(((P + grid - 1) / grid + 31) / 32 * 32);
-        f.pix = (f.chunk + kFusedThreads - 1) / kFusedThreads;
+        f.pix = (f.chunk + threads - 1) / threads;
         TrackLevelBufs &cb = tr->curb(l), &rb = tr->refb(l);
         f.ref_int = rb.intensity;
         f.ref_invd = rb.invd;
@@ -1060,7 +1082,7 @@ static bool launch_gn_fused(yas_tracker *tr, cudaStream_t s) {
     if (!tr->use_fused || !fused_plan(tr, pix, grid)) return false;
     FusedArgs a;
     memset(&a, 0, sizeof(a));
-    fill_levels(tr, grid, a.lv);
+    fill_levels(tr, grid, pix == 0 ? fused_threads<0>() : fused_threads<1>(), a.lv);
     a.L = tr->L;
     a.mode = tr->mode;
     a.angle_th = tr->angle_th;
@@ -1099,7 +1121,7 @@ void gn_batch_item_ctas(yas_tracker *tr, int cta0, int nctas, GNBatchItem *out) 
     memset(out, 0, sizeof(*out));
     out->nctas = std::max(1, std::min(nctas, kFusedMaxCtas));
     out->cta0 = cta0;
-    fill_levels(tr, out->nctas, out->lv);
+    fill_levels(tr, out->nctas, kBatchThreads, out->lv);
     out->L = tr->L;
     out->mode = tr->mode;
     out->angle_th = tr->angle_th;
@@ -1120,11 +1142,11 @@ int gn_batch_capacity() {
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         int lowest = 1 << 30;
         for (auto k : {gn_fused_batch<0>, gn_fused_batch<1>, gn_fused_batch<2>, gn_fused_batch<4>}) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kFusedThreads, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kBatchThreads, 0);
             lowest = std::min(lowest, nb);
         }
         cudaGetLastError();
-        cap[dev] = coop ? std::max(0, std::min(lowest * sms, kFusedMaxCtas)) : -1;
+        cap[dev] = coop ? std::max(0, std::min(std::min(lowest, 1) * sms, kFusedMaxCtas)) : -1;
     }
     return cap[dev];
 }
@@ -1141,7 +1163,7 @@ cudaError_t launch_gn_batch(const GNBatchItem *dev_items, const unsigned short *
     if (grid <= 0 || grid > gn_batch_capacity()) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kFusedThreads);
+    cfg.blockDim = dim3(kBatchThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
