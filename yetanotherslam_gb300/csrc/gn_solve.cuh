@@ -114,21 +114,26 @@ __device__ __forceinline__ bool df_seed_range(DF x) {
 
 // 1 / d: r0 = the hardware's approximate FP32 reciprocal of d.h (relative
 // error below 2^-22), e = 1 - d r0 (1 - fl(d.h r0) is exact: Sterbenz),
-// r = r0 + r0 e, one Newton-Raphson step.  Relative error below 2^-43 in the
-// seed range; outside it an FP64 division (pivots of a Gauss-Newton system
-// stay far inside: its entries are sums of squared image and depth gradients).
+// r = r0 + r0 e, one Newton-Raphson step: relative error below 2^-43.  A
+// pivot outside the seed range is first scaled by 2^64 or 2^-64 (exact) and
+// the reciprocal scaled back, without a branch (pivots of a Gauss-Newton
+// system stay far inside: its entries are sums of squared image and depth
+// gradients).
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 __device__ __forceinline__ DF df_rcp(DF d) {
-    if (!df_seed_range(d)) return df_from_double(1.0 / df_to_double(d));
-    const float r0 = rcp_approx(d.h);
-    const float p = __fmul_rn(d.h, r0);
-    const float pe = __fmaf_rn(d.h, r0, -p);
-    const float e = __fmaf_rn(-d.l, r0, __fsub_rn(__fsub_rn(1.0f, p), pe));
-    return df_fast(r0, __fmul_rn(r0, e));
+    const unsigned ab = __float_as_uint(d.h) & 0x7fffffffu;
+    const float sc = ab <= 0x0da24260u ? 0x1p64f : (ab >= 0x7149f2cau ? 0x1p-64f : 1.0f);
+    const float dh = __fmul_rn(d.h, sc), dl = __fmul_rn(d.l, sc);
+    const float r0 = rcp_approx(dh);
+    const float p = __fmul_rn(dh, r0);
+    const float pe = __fmaf_rn(dh, r0, -p);
+    const float e = __fmaf_rn(-dl, r0, __fsub_rn(__fsub_rn(1.0f, p), pe));
+    const DF r = df_fast(r0, __fmul_rn(r0, e));
+    return DF{__fmul_rn(r.h, sc), __fmul_rn(r.l, sc)};
 }
 
 // a / x: a times the refined reciprocal in the seed range, an FP64 division
@@ -202,7 +207,9 @@ constexpr unsigned kInfBitsF = 0x7f800000u;
 
 // The solve (warp 0; every lane must call it).  Reads g_solve's totals and
 // estimate state, writes the new state and the outputs back to g_solve.
-__device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_level, int level) {
+// Inlined into kernels with registers to spare (gn_solve_inline), called
+// (gn_solve) from the 64-register ones, where inlining adds spills.
+__device__ __forceinline__ void gn_solve_inline(int mode, int no_update, int first_of_level, int level) {
     SolveShared &S = g_solve;
     constexpr unsigned kAll = 0xffffffffu;
     const int lane = (int)(threadIdx.x & 31);
@@ -451,6 +458,10 @@ __device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_leve
         }
     }
     __syncwarp();
+}
+
+__device__ __noinline__ void gn_solve(int mode, int no_update, int first_of_level, int level) {
+    gn_solve_inline(mode, no_update, first_of_level, level);
 }
 
 // Threads 0..31 load the estimate state of `st` into g_solve (the caller sets

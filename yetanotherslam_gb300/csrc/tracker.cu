@@ -900,7 +900,10 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             if (!fold_systems<NT>(rA, rB, nrows, tag, do_icp, do_rgb, st, plain)) return;
             if (t < 32) {
                 if (!do_rgb && t == 0) g_solve.huber_th = huber_threshold_solve();
-                gn_solve(mode, 0, it == 0, l);
+                if constexpr (NT <= 512)
+                    gn_solve_inline(mode, 0, it == 0, l);
+                else
+                    gn_solve(mode, 0, it == 0, l);
             }
             __syncthreads();
             if (g_solve.failed != 0) {
