@@ -44,6 +44,7 @@
 #pragma once
 
 #include <cfloat>
+#include <climits>
 
 #include "yas_track.h"
 
@@ -169,6 +170,7 @@ struct SolveShared {
     float Hh[36], Hl[36], bh[6], bl[6], uh[6], ul[6];
     float stats[3];  // residualSum, numResidual, huber_th (FP32 in the reference)
     float xsh[8], xsl[8];  // solution scatter (undoing the pivot permutation)
+    int perm[8];           // static pivot order: perm[p] = the row pivoted at step p
 };
 __shared__ SolveShared g_solve;
 
@@ -259,41 +261,22 @@ __device__ __forceinline__ void gn_solve_inline(int mode, int no_update, int fir
     {
         const unsigned ab0 = __float_as_uint(a.h) & kAbsMaskF;
         const int key0 = (ism && ei == ej) ? (ab0 > kInfBitsF ? -1 : (int)ab0) : -2;
-        int kd[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) kd[q] = __shfl_sync(kAll, key0, tri_lane(q, q));
-        int pos[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            int rq = 0;
-#pragma unroll
-            for (int r = 0; r < 6; ++r) rq += (kd[r] > kd[q] || (kd[r] == kd[q] && r < q)) ? 1 : 0;
-            pos[q] = rq;
-        }
-        // inverse permutation, the largest key and this lane's pivot rows by
-        // selects (registers, no indexed local arrays)
-        int inv[6];
-#pragma unroll
-        for (int p = 0; p < 6; ++p) {
-            int v = 0;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) v = pos[q] == p ? q : v;
-            inv[p] = v;
-        }
-        int kmax = kd[0];
-#pragma unroll
-        for (int q = 1; q < 6; ++q) kmax = max(kmax, kd[q]);
+        // lane 5q + r' (r' < 5) asks whether row r (the r'-th row other than
+        // q) ranks before row q; the rank of q counts its five answers
+        const int pq = lane / 5, pr0 = lane - 5 * pq, pr = pr0 < pq ? pr0 : pr0 + 1;
+        const int kq = __shfl_sync(kAll, key0, lane < 30 ? tri_lane(pq, pq) : 0);
+        const int kr = __shfl_sync(kAll, key0, lane < 30 ? tri_lane(pr, pr) : 0);
+        const unsigned before = __ballot_sync(kAll, lane < 30 && (kr > kq || (kr == kq && pr < pq)));
+        // perm[p] = the row of rank p
+        if (lane < 6) S.perm[__popc((before >> (5 * lane)) & 0x1fu)] = lane;
+        const int kmax = __reduce_max_sync(kAll, key0 == -2 ? INT_MIN : key0);
+        const int k0 = __shfl_sync(kAll, key0, 0);
+        __syncwarp();
         // no factorisation when the largest diagonal is zero or the first is NaN
-        broke = kmax <= 0 || kd[0] == -1;
+        broke = kmax <= 0 || k0 == -1;
         if (!broke) {
-            int pi = 0, pj = 0;
-#pragma unroll
-            for (int p = 0; p < 6; ++p) {
-                pi = ei == p ? inv[p] : pi;
-                pj = ej == p ? inv[p] : pj;
-            }
-            pi = ism || isb ? pi : 0;
-            pj = ism ? pj : 0;
+            const int pi = ism || isb ? S.perm[ei] : 0;
+            const int pj = ism ? S.perm[ej] : 0;
             const int src = ism ? (pi >= pj ? tri_lane(pi, pj) : tri_lane(pj, pi)) : (isb ? 21 + pi : lane);
             a = df_shfl(a, src);
             if (isb) orig = pi;
