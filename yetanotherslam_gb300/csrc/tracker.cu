@@ -293,11 +293,10 @@ __device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, float b0,
 // (floor(fx x / z + cx + 0.5)), and the gates |n_c x n_m| < sin 20 deg,
 // |v_m - v_c| <= dist_th, both normals valid.  On success vl, nl, vc and the
 // point-to-plane residual r = n_m . (v_c - v_m) are set.
-__device__ __forceinline__ bool icp_match(const float *T, const LevelCam &c, const float4 *__restrict__ ref_vmap,
-                                          const float4 *__restrict__ ref_nmap, const float4 *__restrict__ cur_vmap,
-                                          const float4 *__restrict__ cur_nmap, int k, float angle_th, float dist_th,
-                                          float3 &vl, float3 &nl, float4 &vc, float &r) {
-    const float4 vm = __ldg(ref_vmap + k);
+__device__ __forceinline__ bool icp_match_vm(const float *T, const LevelCam &c, const float4 vm,
+                                             const float4 *__restrict__ ref_nmap, const float4 *__restrict__ cur_vmap,
+                                             const float4 *__restrict__ cur_nmap, int k, float angle_th, float dist_th,
+                                             float3 &vl, float3 &nl, float4 &vc, float &r) {
     if (!(vm.w >= 0.0f)) return false;
     vl = make_float3(__fadd_rn(dot3_rn(T[0], T[1], T[2], vm.x, vm.y, vm.z), T[3]),
                      __fadd_rn(dot3_rn(T[4], T[5], T[6], vm.x, vm.y, vm.z), T[7]),
@@ -322,6 +321,12 @@ __device__ __forceinline__ bool icp_match(const float *T, const LevelCam &c, con
     if (!(angle < angle_th && dist <= dist_th && nm.w > 0.0f && nc.w > 0.0f)) return false;
     r = dot3_rn(nl.x, nl.y, nl.z, __fsub_rn(vc.x, vl.x), __fsub_rn(vc.y, vl.y), __fsub_rn(vc.z, vl.z));
     return true;
+}
+__device__ __forceinline__ bool icp_match(const float *T, const LevelCam &c, const float4 *__restrict__ ref_vmap,
+                                          const float4 *__restrict__ ref_nmap, const float4 *__restrict__ cur_vmap,
+                                          const float4 *__restrict__ cur_nmap, int k, float angle_th, float dist_th,
+                                          float3 &vl, float3 &nl, float4 &vc, float &r) {
+    return icp_match_vm(T, c, __ldg(ref_vmap + k), ref_nmap, cur_vmap, cur_nmap, k, angle_th, dist_th, vl, nl, vc, r);
 }
 
 // The ICP row [n, v x n | r] of a matched pair, accumulated into the 28
@@ -604,17 +609,17 @@ __device__ __forceinline__ bool poll_continue(GNState *st, unsigned spin, unsign
     return true;
 }
 
-// Pass A for one pixel: the photometric residual (kept in registers for pass
-// B) and the ICP products, accumulated as gn_pass_a does.
-__device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float *sT, const float *sRK, int k,
-                                              bool do_rgb, bool do_icp, float angle_th, float dist_th,
-                                              float acc[32], float4 &res, float3 &p) {
+// Pass A for one pixel whose reference inverse depth and model vertex are
+// already loaded: the photometric residual (kept in registers for pass B)
+// and the ICP products, accumulated as gn_pass_a does.
+__device__ __forceinline__ void fused_pixel_a_pre(const FusedLevel &lv, const float *sT, const float *sRK, int k,
+                                                  bool do_rgb, bool do_icp, float angle_th, float dist_th,
+                                                  float zinv, float4 vm, float acc[32], float4 &res, float3 &p) {
     const LevelCam &c = lv.c;
     const int y = k / c.w, x = k - y * c.w;
     res = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
     p = make_float3(0.0f, 0.0f, 1.0f);
     if (do_rgb) {
-        const float zinv = __ldg(lv.ref_invd + k);
         if (zinv > 0.0f) {
             const float z = __fdiv_rn(1.0f, zinv);
             p = warp_ref_point(sRK, sT, x, y, z);
@@ -637,9 +642,18 @@ __device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float 
         float3 vl, nl;
         float4 vc;
         float r;
-        if (icp_match(sT, c, lv.ref_vmap, lv.ref_nmap, lv.cur_vmap, lv.cur_nmap, k, angle_th, dist_th, vl, nl, vc, r))
+        if (icp_match_vm(sT, c, vm, lv.ref_nmap, lv.cur_vmap, lv.cur_nmap, k, angle_th, dist_th, vl, nl, vc, r))
             icp_accumulate(vl, nl, r, acc);
     }
+}
+
+// Pass A for one pixel: the photometric residual (kept in registers for pass
+// B) and the ICP products, accumulated as gn_pass_a does.
+__device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float *sT, const float *sRK, int k,
+                                              bool do_rgb, bool do_icp, float angle_th, float dist_th,
+                                              float acc[32], float4 &res, float3 &p) {
+    fused_pixel_a_pre(lv, sT, sRK, k, do_rgb, do_icp, angle_th, dist_th, do_rgb ? __ldg(lv.ref_invd + k) : 0.0f,
+                      do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f), acc, res, p);
 }
 
 // Pass B for one pixel kept from pass A (gn_pass_b's products).
@@ -850,6 +864,18 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             float4 res[PIX > 0 ? PIX : 1];
             float3 pp[PIX > 0 ? PIX : 1];
             if constexpr (PIX > 0) {
+                // the pose-independent reference loads of every pixel first, so
+                // they are in flight together
+                float zi[PIX];
+                float4 vm[PIX];
+#pragma unroll
+                for (int q = 0; q < PIX; ++q) {
+                    const int off = q * NT + t;
+                    const int k = base + off;
+                    const bool own = q < lv.pix && off < lv.chunk && k < n;
+                    zi[q] = own && do_rgb ? __ldg(lv.ref_invd + k) : 0.0f;
+                    vm[q] = own && do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                }
 #pragma unroll
                 for (int q = 0; q < PIX; ++q) {
                     res[q] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
@@ -857,7 +883,8 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     const int off = q * NT + t;
                     const int k = base + off;
                     if (q < lv.pix && off < lv.chunk && k < n)
-                        fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, res[q], pp[q]);
+                        fused_pixel_a_pre(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, zi[q], vm[q], acc,
+                                          res[q], pp[q]);
                 }
             } else {
 #pragma unroll 2
