@@ -827,8 +827,8 @@ __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, co
 // owns at most PIX pixels per level (off = s * NT + thread, NT threads) and
 // keeps their residuals in registers for pass B; PIX == 0: any number of
 // pixels, residuals through `res4` (pass B then recomputes the warped point,
-// as gn_pass_b does).
-template <int PIX, int NT>
+// as gn_pass_b does), G pixels' reference loads at a time.
+template <int PIX, int NT, int G>
 __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mode, float angle_th, float dist_th,
                                             unsigned long long *rows, float4 *res4, GNState *st, unsigned cta,
                                             unsigned nrows) {
@@ -887,14 +887,32 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                                           res[q], pp[q]);
                 }
             } else {
-#pragma unroll 2
-                for (int off = t; off < lv.chunk; off += NT) {
-                    const int k = base + off;
-                    if (k >= n) break;
-                    float4 r4;
-                    float3 p3;
-                    fused_pixel_a(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, acc, r4, p3);
-                    if (do_rgb) res4[k] = r4;
+                // pixels off = t, t + NT, ... in groups of G, each group's
+                // reference loads first (the same pixels in the same order as
+                // one at a time); G = 2 in the batched schedules, whose CTAs
+                // own tens of pixels per thread, G = 1 where a second
+                // pixel's registers would spill (1024 threads, 64 registers)
+#pragma unroll 1
+                for (int off0 = t; off0 < lv.chunk; off0 += G * NT) {
+                    float zi[G];
+                    float4 vm[G];
+#pragma unroll
+                    for (int q = 0; q < G; ++q) {
+                        const int off = off0 + q * NT, k = base + off;
+                        const bool own = off < lv.chunk && k < n;
+                        zi[q] = own && do_rgb ? __ldg(lv.ref_invd + k) : 0.0f;
+                        vm[q] = own && do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                    }
+#pragma unroll
+                    for (int q = 0; q < G; ++q) {
+                        const int off = off0 + q * NT, k = base + off;
+                        if (off >= lv.chunk || k >= n) break;
+                        float4 r4;
+                        float3 p3;
+                        fused_pixel_a_pre(lv, g_solve.Tf, sRK, k, do_rgb, do_icp, angle_th, dist_th, zi[q], vm[q], acc,
+                                          r4, p3);
+                        if (do_rgb) res4[k] = r4;
+                    }
                 }
             }
             fused_publish_row<NT>(acc, rA + cta * 32, tag);
@@ -910,15 +928,25 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     for (int q = 0; q < PIX; ++q)
                         if (res[q].w > 0.0f) fused_pixel_b(lv.c, th, res[q], pp[q], acc);
                 } else {
-#pragma unroll 2
-                    for (int off = t; off < lv.chunk; off += NT) {
-                        const int k = base + off;
-                        if (k >= n) break;
-                        const float4 r4 = res4[k];
-                        if (r4.w > 0.0f) {
-                            const int y = k / lv.c.w, x = k - y * lv.c.w;
-                            const float3 p3 = warp_ref_point(sRK, g_solve.Tf, x, y, 1.0f / __ldg(lv.ref_invd + k));
-                            fused_pixel_b(lv.c, th, r4, p3, acc);
+#pragma unroll 1
+                    for (int off0 = t; off0 < lv.chunk; off0 += G * NT) {
+                        float4 r4[G];
+                        float zi[G];
+#pragma unroll
+                        for (int q = 0; q < G; ++q) {
+                            const int off = off0 + q * NT, k = base + off;
+                            const bool own = off < lv.chunk && k < n;
+                            r4[q] = own ? res4[k] : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                            zi[q] = own ? __ldg(lv.ref_invd + k) : 1.0f;
+                        }
+#pragma unroll
+                        for (int q = 0; q < G; ++q) {
+                            const int k = base + off0 + q * NT;
+                            if (r4[q].w > 0.0f) {
+                                const int y = k / lv.c.w, x = k - y * lv.c.w;
+                                const float3 p3 = warp_ref_point(sRK, g_solve.Tf, x, y, 1.0f / zi[q]);
+                                fused_pixel_b(lv.c, th, r4[q], p3, acc);
+                            }
                         }
                     }
                 }
@@ -949,7 +977,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
 // The fused schedule of one tracker over the whole grid.
 template <int PIX>
 __global__ void __launch_bounds__(fused_threads<PIX>(), 1) gn_fused(const __grid_constant__ FusedArgs a) {
-    gn_schedule<PIX, fused_threads<PIX>()>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, a.res4, a.st, blockIdx.x, gridDim.x);
+    gn_schedule<PIX, fused_threads<PIX>(), 1>(a.lv, a.L, a.mode, a.angle_th, a.dist_th, a.rows, a.res4, a.st, blockIdx.x, gridDim.x);
 }
 
 // Fused schedules of a batch of trackers in one launch: CTA b runs for item
@@ -961,7 +989,7 @@ template <int PIX>
 __global__ void __launch_bounds__(kBatchThreads, 1) gn_fused_batch(const GNBatchItem *__restrict__ items,
                                                                     const unsigned short *__restrict__ cta_item) {
     const GNBatchItem &it = items[cta_item[blockIdx.x]];
-    gn_schedule<PIX, kBatchThreads>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st,
+    gn_schedule<PIX, kBatchThreads, 2>(it.lv, it.L, it.mode, it.angle_th, it.dist_th, it.rows, it.res4, it.st,
                                     blockIdx.x - (unsigned)it.cta0, (unsigned)it.nctas);
 }
 
