@@ -286,6 +286,13 @@ YAS_API int yas_tracker_is_good(yas_tracker *tr, int *out);
  * stats[4] = {sum r^2 used for the error, residual count, rgb sigma, icp count}. */
 YAS_API int yas_tracker_compute_step(yas_tracker *tr, int level, const yas_pose *T, double *H,
                                      double *b, double *stats);
+/* The last Gauss-Newton solve of the tracker's last GetTransform or
+ * compute_step (no counterpart in the reference; for inspection and tests):
+ * the combined system H (36, row-major) and b (6) it solved, the update x
+ * (6: translation then rotation, LDLT(H).solve(b)) and the estimate after
+ * it (exp(x) * the estimate before).  Any pointer may be null; waits for the
+ * tracker's stream. */
+YAS_API int yas_tracker_last_solve(yas_tracker *tr, double *H, double *b, double *update, yas_pose *estimate);
 /* Device pointers of pyramid level buffers (for inspection/tests).
  * which: 0 cur intensity, 1 cur gx, 2 cur gy, 3 cur inv-depth, 4 cur vmap,
  * 5 cur nmap, 6 ref intensity, 7 ref inv-depth, 8 ref vmap, 9 ref nmap. */

@@ -225,3 +225,26 @@ def test_seeded_division_against_ieee(native, cuda):
     assert rel.max() <= 2.0 ** -43, rel.max()
     inside = (np.abs(x) > 1e-30) & (np.abs(x) < 1e30)
     print(f"df_div: max relative error {rel[inside].max():.3g} in the seed range, {rel[~inside].max():.3g} above it")
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_double_float_solve_against_fp64(cuda, mode):
+    """The device solve (double-float, 48 significant bits; gn_solve.cuh) on
+    the system of a real Gauss-Newton iteration, against the oracle's FP64
+    LDLT (Eigen's pivot search at every step) and SE(3) exponential on the
+    same H and b (RGBDTracking.cu:185-197).  Bars: the update within
+    64 * cond(H) * 2^-47 of the FP64 solution, relative to its norm (the
+    backward-stable LDL^T bound at double-float precision), and the estimate
+    exp(x) within 1e-13 of the FP64 exponential of the device's own x."""
+    tr, _, _ = _setup(mode, levels=1, iters=(1,))
+    tr.set_schedule(True)
+    tr.GetTransform(np.eye(4), False)
+    H, b, x, est = tr.last_solve()
+    assert np.all(np.isfinite(H)) and np.abs(H).max() > 0
+    x_ref = oracle.ldlt_solve(H, b)
+    cond = np.linalg.cond(H)
+    rel = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+    print(f"mode {mode}: cond(H) {cond:.3g}, update relative error {rel:.3g}, |x| {np.linalg.norm(x_ref):.3g}")
+    assert rel <= 64.0 * cond * 2.0 ** -47, (rel, cond)
+    T_ref = oracle.se3_exp(x)  # estimate before the update is the identity
+    assert np.abs(est - T_ref).max() <= 1e-13, np.abs(est - T_ref).max()

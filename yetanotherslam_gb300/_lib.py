@@ -163,6 +163,7 @@ _SIGS = {
     "yas_tracker_set_schedule": [_P, _I],
     "yas_tracker_compute_step": [_P, _I, C.POINTER(Pose), _P, _P, _P],
     "yas_tracker_level_buffer": [_P, _I, _I, _PP, _PI, _PI, _PI],
+    "yas_tracker_last_solve": [_P, _P, _P, _P, C.POINTER(Pose)],
     "yas_session_config_default": [C.POINTER(SessionConfig), _I, _I, C.POINTER(Intrinsics), _I, _I,
                                    C.c_float, C.c_float, _I],
     "yas_session_create": [_PP, C.POINTER(SessionConfig), _P],

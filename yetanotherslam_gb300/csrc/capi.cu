@@ -1297,6 +1297,22 @@ YAS_API int yas_tracker_compute_step(yas_tracker *tr, int level, const yas_pose 
     return YAS_OK;
 }
 
+YAS_API int yas_tracker_last_solve(yas_tracker *tr, double *H, double *b, double *update, yas_pose *estimate) {
+    if (!tr) return YAS_ERR_BAD_ARG;
+    YAS_TRY_CUDA(cudaStreamSynchronize(tr->stream));
+    YAS_TRY_CUDA(cudaMemcpy(tr->state_host, tr->state, sizeof(GNState), cudaMemcpyDeviceToHost));
+    const GNState &st = *tr->state_host;
+    if (H)
+        for (int i = 0; i < 36; ++i) H[i] = st.H[i];
+    if (b)
+        for (int i = 0; i < 6; ++i) b[i] = st.b[i];
+    if (update)
+        for (int i = 0; i < 6; ++i) update[i] = st.last_update[i];
+    if (estimate)
+        for (int i = 0; i < 12; ++i) estimate->m[i] = st.est[i];
+    return YAS_OK;
+}
+
 YAS_API int yas_tracker_level_buffer(yas_tracker *tr, int level, int which, const void **dev_ptr, int *width,
                                      int *height, int *pitch_bytes) {
     if (!tr || !dev_ptr || level < 0 || level >= tr->L || which < 0 || which > 9) return YAS_ERR_BAD_ARG;

@@ -384,6 +384,15 @@ class RGBDTracking:
                b.ctypes.data, st.ctypes.data)
         return H.reshape(6, 6), b, st
 
+    def last_solve(self):
+        """(H 6x6, b, update x, estimate 4x4) of the last Gauss-Newton solve."""
+        H = np.zeros(36)
+        b = np.zeros(6)
+        x = np.zeros(6)
+        est = L.Pose()
+        L.call("yas_tracker_last_solve", self.handle, H.ctypes.data, b.ctypes.data, x.ctypes.data, C.byref(est))
+        return H.reshape(6, 6), b, x, L.pose_to(est)
+
     def level_buffer(self, level: int, which: int) -> DeviceArray:
         ptr = C.c_void_p()
         w, h, p = C.c_int(), C.c_int(), C.c_int()
