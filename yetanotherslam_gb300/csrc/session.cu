@@ -17,7 +17,9 @@
 // step check and pose composition run on the device, and fusion kernels read
 // a skip flag, so a rejected frame changes nothing.  The raycast reuses the
 // visible-block list of the previous fusion, which was built at exactly the
-// pose the raycast uses.  Two graphs alternate because the reference and
+// pose the raycast uses, so its z-range tiles are filled right after that
+// fusion's visibility pass, beside its integration, and the next frame starts
+// with the march.  Two graphs alternate because the reference and
 // current pyramids swap roles every frame (RGBDTracking::SwapFrameBuffer,
 // RGBDTracking.cu:294-303).
 // Deliberate difference: a NaN in the solve skips fusion and reports
@@ -134,6 +136,10 @@ struct yas_session {
     bool own_stream = false;
     yas_map *map = nullptr;
     yas_raycaster *rc = nullptr;
+    // z-range tiles of the next frame's raycast (the session's own, so calls on
+    // its raycaster between frames leave them alone): filled after each
+    // frame's visibility pass, which is at the pose the next raycast uses
+    RaycastBuffers zt = {};
     yas_tracker *tr = nullptr;
     uint8_t *d_rgb = nullptr;
     uint16_t *d_depth = nullptr;
@@ -175,16 +181,40 @@ static void prof_mark(void *ctx, int id) {
 enum { kStImage = 0, kStDepth = 1, kStZrange = 2, kStMarch = 3, kStModel = 4, kStGnInit = 5,
        kStFinalize = 6, kStAllocate = 7, kStVisible = 8, kStIntegrate = 9, kStEnd = 99 };
 
+// The next raycast's z-range tiles (RayTraceEngine.cu:58-264) from the map's
+// visible list and the frame pose pair: both are final once a frame's
+// visibility pass has run, and nothing changes them before the next frame's
+// march.
+static void enqueue_zrange(yas_session *s, cudaStream_t st) {
+    prof_mark(s, kStZrange);
+    launch_zrange(map_view(s->map), s->rc->cam, &s->fs->pp, s->zt, nullptr, st);
+}
+
+// Allocation, visibility and integration (Fuse, VoxelMap.cu:517-786), then the
+// next frame's z-range tiles: beside integration on the side stream (they
+// need only the visible list and the pose), after it when profiling.
 static void enqueue_fusion(yas_session *s, const int *skip) {
     MapDev v = map_view(s->map);
     const int fmt = s->map->cfg.voxel_format;
+    cudaStream_t st = s->stream;
     prof_mark(s, kStAllocate);
-    launch_allocate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream);
+    launch_allocate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st);
     prof_mark(s, kStVisible);
-    launch_visible(v, s->cam, &s->fs->pp, skip, s->stream);
+    launch_visible(v, s->cam, &s->fs->pp, skip, st);
+    const bool side = s->side && !s->profiling;
+    if (side) {
+        cudaEventRecord(s->ev_fork, st);
+        cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+        enqueue_zrange(s, s->side);
+    }
     prof_mark(s, kStIntegrate);
-    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, s->stream,
-                     s->shape.integrate_ctas);
+    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st, s->shape.integrate_ctas);
+    if (side) {
+        cudaEventRecord(s->ev_join, s->side);
+        cudaStreamWaitEvent(st, s->ev_join, 0);
+    } else {
+        enqueue_zrange(s, st);
+    }
 }
 
 static void enqueue_first_frame(yas_session *s) {
@@ -197,15 +227,14 @@ static void enqueue_first_frame(yas_session *s) {
 }
 
 // Raycast of the map at the last pose and the model pyramid built from it
-// (Tracking.cpp:164-169): reads the map and the pose pair, writes the
-// reference set's vertex/normal maps only.
+// (Tracking.cpp:164-169): reads the map, the pose pair and the z-range tiles
+// the previous frame's fusion left, writes the reference set's vertex/normal
+// maps only.
 static void enqueue_raycast_branch(yas_session *s, cudaStream_t st) {
     yas_tracker *tr = s->tr;
     MapDev v = map_view(s->map);
-    prof_mark(s, kStZrange);
-    launch_zrange(v, s->rc->cam, &s->fs->pp, s->rc->rb, nullptr, st);
     prof_mark(s, kStMarch);
-    launch_march(v, s->map->cfg.voxel_format, s->rc->cam, &s->fs->pp, s->rc->rb, tr->refb(0).vmap, s->cfg.width,
+    launch_march(v, s->map->cfg.voxel_format, s->rc->cam, &s->fs->pp, s->zt, tr->refb(0).vmap, s->cfg.width,
                  nullptr, st, s->shape.march_warps_x);
     prof_mark(s, kStModel);
     tracker_model(tr, st);
@@ -447,6 +476,22 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
     int st = yas_map_create(&s->map, &cfg->map, &cfg->K, s->stream);
     if (st == YAS_OK) st = yas_raycaster_create(&s->rc, cfg->width, cfg->height, &cfg->K, s->stream);
     if (st == YAS_OK) {
+        RaycastBuffers &z = s->zt;
+        z.w = cfg->width;
+        z.h = cfg->height;
+        z.zw = (cfg->width + 7) / 8;
+        z.zh = (cfg->height + 7) / 8;
+        z.fw = (cfg->width + (1 << kFineShift) - 1) >> kFineShift;
+        z.fh = (cfg->height + (1 << kFineShift) - 1) >> kFineShift;
+        const size_t nz = (size_t)z.zw * z.zh;
+        if (cudaMalloc(&z.znear, nz * 4) != cudaSuccess || cudaMalloc(&z.zfar, nz * 4) != cudaSuccess ||
+            cudaMalloc(&z.queue, sizeof(unsigned)) != cudaSuccess ||
+            cudaMalloc(&z.fnear, (size_t)z.fw * z.fh * 4) != cudaSuccess) {
+            cudaGetLastError();
+            st = YAS_ERR_OOM;
+        }
+    }
+    if (st == YAS_OK) {
         const double K[9] = {cfg->K.fx, 0, cfg->K.cx, 0, cfg->K.fy, cfg->K.cy, 0, 0, 1};
         st = yas_tracker_create(&s->tr, cfg->width, cfg->height, K, cfg->num_levels, cfg->iterations, cfg->mode,
                                 s->stream);
@@ -493,6 +538,10 @@ YAS_API int yas_session_destroy(yas_session *s) {
     if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
     if (s->tr) yas_tracker_destroy(s->tr);
     if (s->rc) yas_raycaster_destroy(s->rc);
+    cudaFree(s->zt.znear);
+    cudaFree(s->zt.zfar);
+    cudaFree(s->zt.queue);
+    cudaFree(s->zt.fnear);
     if (s->map) yas_map_destroy(s->map);
     cudaFree(s->d_rgb);
     cudaFree(s->d_depth);
@@ -590,8 +639,10 @@ YAS_API int yas_session_new_submap(yas_session *s, yas_map **out_previous) {
     }
     if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
     s->post_exec = nullptr;
-    // the frame's pose relative to the new submap restarts at the identity
+    // the frame's pose relative to the new submap restarts at the identity;
+    // the next raycast's z-range tiles are the new (empty) map's
     frame_begin_kernel<<<1, 32, 0, s->stream>>>(s->fs, pose_identity(), nm->hdr);
+    launch_zrange(map_view(nm), s->rc->cam, &s->fs->pp, s->zt, nullptr, s->stream);
     YAS_TRY_CUDA(cudaGetLastError());
     YAS_TRY_CUDA(cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, s->stream));
     YAS_TRY_CUDA(cudaStreamSynchronize(s->stream));
