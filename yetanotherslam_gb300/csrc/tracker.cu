@@ -516,7 +516,7 @@ __global__ void gn_init_kernel(GNState *st, Pose64 init, int L, PassArgs kargs) 
 
 // ---------------------------------------------------------------- fused schedule
 // One cooperative launch runs every Gauss-Newton iteration of every level
-// (GetTransform's loops, RGBDTracking.cu:161-208), one 512-thread CTA per SM,
+// (GetTransform's loops, RGBDTracking.cu:161-208), one CTA per SM,
 // CTA c owning the pixel range [c * chunk, (c + 1) * chunk) of each level.
 // Nothing is released by one CTA to the others: each CTA publishes its row
 // of partial sums as tagged 64-bit words {value, tag} (tag = launch epoch and
@@ -753,7 +753,8 @@ __device__ __forceinline__ bool fold_moments(const unsigned long long *rows, uns
 // solve's pass A totals 0..28 and of the photometric system (columns 0..27 of
 // rows B) into its pass B totals 0..27 (zero for a term the mode does not
 // use).  Thread t folds column t % 64 over the rows of subset t / 64
-// (compensated FP32), then a butterfly over the 8 subsets of each column;
+// (compensated FP32), then a butterfly over the subsets of each column (8 at
+// 512 threads, 16 at 1024);
 // each total is kept as a double-float pair.  False on abort or timeout.
 template <int NT>
 __device__ __forceinline__ bool fold_systems(const unsigned long long *rowsA, const unsigned long long *rowsB,
