@@ -252,6 +252,11 @@ __device__ __forceinline__ void gn_solve_inline(int mode, int no_update, int fir
         __syncwarp();
         return;
     }
+    // acceptance on the error measured before the update, decided by every
+    // lane now so that its division and square root overlap the factorisation
+    const float error = sqrtf(residualSum) / (numResidual + 6.0f);
+    const float last = first_of_level ? FLT_MAX : S.last_error;
+    const bool accept = error < last;
     // ---- LDL^T on [H | b] with a static pivot order: the diagonal's initial
     // |values|, largest first (first on ties), applied as one symmetric
     // permutation; the factorisation itself divides through the refined
@@ -418,19 +423,13 @@ __device__ __forceinline__ void gn_solve_inline(int mode, int no_update, int fir
     const DF o = df_fma(E0, DF{S.esth[q], S.estl[q]},
                         df_fma(E1, DF{S.esth[4 + q], S.estl[4 + q]},
                                df_fma(E2, DF{S.esth[8 + q], S.estl[8 + q]}, tl ? ti : df(0.0f))));
-    // ---- acceptance on the error measured before the update
-    const float error = sqrtf(residualSum) / (numResidual + 6.0f);
-    int accept = 0;
+    // ---- the new state
     if (lane == 0) {
-        const float last = first_of_level ? FLT_MAX : S.last_error;
-        accept = error < last;
         S.last_error = accept ? error : last;
         S.n_success += accept ? 1 : 0;
         S.n_iter += 1;
         S.level_of_last = level;
     }
-    accept = __shfl_sync(kAll, accept, 0);
-    __syncwarp();
     if (lane < 12) {
         S.esth[lane] = o.h;
         S.estl[lane] = o.l;

@@ -138,9 +138,15 @@ __device__ __forceinline__ float raw_depth(const void *src, int is_u16, int pitc
     return reinterpret_cast<const float *>(static_cast<const char *>(src) + (size_t)y * pitch)[x];
 }
 
-// Level 0 depth: metres (optional), inverse depth, vertex and normal maps.
+// Depth of an inverse depth as the photometric warp uses it (1 / invd, one
+// IEEE division), 0 where the inverse depth is invalid.
+__device__ __forceinline__ float warp_depth_of(float invz) { return invz > 0.0f ? 1.0f / invz : 0.0f; }
+
+// Level 0 depth: metres (optional), inverse depth, its reciprocal, vertex and
+// normal maps.
 __global__ void depth_level0_kernel(const void *__restrict__ src, int is_u16, int pitch, float scale,
-                                    LevelCam c, float *depth_m, float *invd, float4 *vmap, float4 *nmap) {
+                                    LevelCam c, float *depth_m, float *invd, float *zmap, float4 *vmap,
+                                    float4 *nmap) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= c.w || y >= c.h) return;
@@ -148,6 +154,7 @@ __global__ void depth_level0_kernel(const void *__restrict__ src, int is_u16, in
     const float iz = inv_depth_of(z);
     if (depth_m) depth_m[y * c.w + x] = z;
     invd[y * c.w + x] = iz;
+    zmap[y * c.w + x] = warp_depth_of(iz);
     const float4 v00 = vertex_of(iz, x, y, c);
     vmap[y * c.w + x] = v00;
     float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
@@ -165,13 +172,14 @@ __device__ __forceinline__ float invd_down(const float *prev, int pw, int x, int
     return __ldg(prev + (size_t)(2 * y) * pw + 2 * x);
 }
 
-__global__ void depth_pyr_kernel(const float *__restrict__ prev, int pw, LevelCam c, float *invd,
+__global__ void depth_pyr_kernel(const float *__restrict__ prev, int pw, LevelCam c, float *invd, float *zmap,
                                  float4 *vmap, float4 *nmap) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= c.w || y >= c.h) return;
     const float iz = invd_down(prev, pw, x, y, c.w, c.h);
     invd[y * c.w + x] = iz;
+    zmap[y * c.w + x] = warp_depth_of(iz);
     const float4 v00 = vertex_of(iz, x, y, c);
     vmap[y * c.w + x] = v00;
     float4 n = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
@@ -250,14 +258,14 @@ void launch_image_level(const float *prev, int pw, int ph, int w, int h, float *
 }
 
 void launch_depth_level0(const void *src, int is_u16, int pitch, float scale, const LevelCam &c,
-                         float *depth_m, float *invd, float4 *vmap, float4 *nmap, cudaStream_t s) {
+                         float *depth_m, float *invd, float *zmap, float4 *vmap, float4 *nmap, cudaStream_t s) {
     depth_level0_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(src, is_u16, pitch, scale, c, depth_m, invd,
-                                                                 vmap, nmap);
+                                                                 zmap, vmap, nmap);
 }
 
-void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float4 *vmap,
+void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float *zmap, float4 *vmap,
                         float4 *nmap, cudaStream_t s) {
-    depth_pyr_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(prev, pw, c, invd, vmap, nmap);
+    depth_pyr_kernel<<<grid2(c.w, c.h), dim3(32, 8), 0, s>>>(prev, pw, c, invd, zmap, vmap, nmap);
 }
 
 // ---------------------------------------------------------------- shading

@@ -609,19 +609,19 @@ __device__ __forceinline__ bool poll_continue(GNState *st, unsigned spin, unsign
     return true;
 }
 
-// Pass A for one pixel whose reference inverse depth and model vertex are
+// Pass A for one pixel whose reference depth (1 / inverse depth, 0 where
+// that is invalid: the same division gn_pass_a makes) and model vertex are
 // already loaded: the photometric residual (kept in registers for pass B)
 // and the ICP products, accumulated as gn_pass_a does.
 __device__ __forceinline__ void fused_pixel_a_pre(const FusedLevel &lv, const float *sT, const float *sRK, int k,
                                                   bool do_rgb, bool do_icp, float angle_th, float dist_th,
-                                                  float zinv, float4 vm, float acc[32], float4 &res, float3 &p) {
+                                                  float z, float4 vm, float acc[32], float4 &res, float3 &p) {
     const LevelCam &c = lv.c;
     const int y = k / c.w, x = k - y * c.w;
     res = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
     p = make_float3(0.0f, 0.0f, 1.0f);
     if (do_rgb) {
-        if (zinv > 0.0f) {
-            const float z = __fdiv_rn(1.0f, zinv);
+        if (z > 0.0f) {
             p = warp_ref_point(sRK, sT, x, y, z);
             float u, v;
             if (rgb_project(c, p, u, v)) {
@@ -652,7 +652,7 @@ __device__ __forceinline__ void fused_pixel_a_pre(const FusedLevel &lv, const fl
 __device__ __forceinline__ void fused_pixel_a(const FusedLevel &lv, const float *sT, const float *sRK, int k,
                                               bool do_rgb, bool do_icp, float angle_th, float dist_th,
                                               float acc[32], float4 &res, float3 &p) {
-    fused_pixel_a_pre(lv, sT, sRK, k, do_rgb, do_icp, angle_th, dist_th, do_rgb ? __ldg(lv.ref_invd + k) : 0.0f,
+    fused_pixel_a_pre(lv, sT, sRK, k, do_rgb, do_icp, angle_th, dist_th, do_rgb ? __ldg(lv.ref_z + k) : 0.0f,
                       do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f), acc, res, p);
 }
 
@@ -865,8 +865,8 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
             float4 res[PIX > 0 ? PIX : 1];
             float3 pp[PIX > 0 ? PIX : 1];
             if constexpr (PIX > 0) {
-                // the pose-independent reference loads of every pixel first, so
-                // they are in flight together
+                // the pose-independent reference loads (depth, model vertex) of
+                // every pixel first, so they are in flight together
                 float zi[PIX];
                 float4 vm[PIX];
 #pragma unroll
@@ -874,7 +874,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     const int off = q * NT + t;
                     const int k = base + off;
                     const bool own = q < lv.pix && off < lv.chunk && k < n;
-                    zi[q] = own && do_rgb ? __ldg(lv.ref_invd + k) : 0.0f;
+                    zi[q] = own && do_rgb ? __ldg(lv.ref_z + k) : 0.0f;
                     vm[q] = own && do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
                 }
 #pragma unroll
@@ -901,7 +901,7 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                     for (int q = 0; q < G; ++q) {
                         const int off = off0 + q * NT, k = base + off;
                         const bool own = off < lv.chunk && k < n;
-                        zi[q] = own && do_rgb ? __ldg(lv.ref_invd + k) : 0.0f;
+                        zi[q] = own && do_rgb ? __ldg(lv.ref_z + k) : 0.0f;
                         vm[q] = own && do_icp ? __ldg(lv.ref_vmap + k) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
                     }
 #pragma unroll
@@ -938,14 +938,14 @@ __device__ __forceinline__ void gn_schedule(const FusedLevel *lvs, int L, int mo
                             const int off = off0 + q * NT, k = base + off;
                             const bool own = off < lv.chunk && k < n;
                             r4[q] = own ? res4[k] : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-                            zi[q] = own ? __ldg(lv.ref_invd + k) : 1.0f;
+                            zi[q] = own ? __ldg(lv.ref_z + k) : 1.0f;
                         }
 #pragma unroll
                         for (int q = 0; q < G; ++q) {
                             const int k = base + off0 + q * NT;
                             if (r4[q].w > 0.0f) {
                                 const int y = k / lv.c.w, x = k - y * lv.c.w;
-                                const float3 p3 = warp_ref_point(sRK, g_solve.Tf, x, y, 1.0f / zi[q]);
+                                const float3 p3 = warp_ref_point(sRK, g_solve.Tf, x, y, zi[q]);
                                 fused_pixel_b(lv.c, th, r4[q], p3, acc);
                             }
                         }
@@ -1126,6 +1126,7 @@ static void fill_levels(yas_tracker *tr, int grid, int threads, FusedLevel *lv) 
         TrackLevelBufs &cb = tr->curb(l), &rb = tr->refb(l);
         f.ref_int = rb.intensity;
         f.ref_invd = rb.invd;
+        f.ref_z = rb.z;
         f.ref_vmap = rb.vmap;
         f.ref_nmap = rb.nmap;
         f.cur_int = cb.intensity;
@@ -1262,9 +1263,10 @@ int tracker_alloc(yas_tracker *tr) {
             TrackLevelBufs &b = tr->set[sidx][l];
             b.intensity = (float *)grab(n * 4);
             b.invd = (float *)grab(n * 4);
+            b.z = (float *)grab(n * 4);
             b.vmap = (float4 *)grab(n * 16);
             b.nmap = (float4 *)grab(n * 16);
-            if (!b.intensity || !b.invd || !b.vmap || !b.nmap) return YAS_ERR_OOM;
+            if (!b.intensity || !b.invd || !b.z || !b.vmap || !b.nmap) return YAS_ERR_OOM;
         }
         tr->gx[l] = (float *)grab(n * 4);
         tr->gy[l] = (float *)grab(n * 4);
@@ -1322,9 +1324,11 @@ void tracker_image(yas_tracker *tr, const uint8_t *src, int channels, int pitch,
 void tracker_depth(yas_tracker *tr, const void *src, int is_u16, int pitch, float scale, float *depth_m,
                    bool reference, cudaStream_t s) {
     TrackLevelBufs *B = reference ? tr->set[1 - tr->cur] : tr->set[tr->cur];
-    launch_depth_level0(src, is_u16, pitch, scale, tr->cam[0], depth_m, B[0].invd, B[0].vmap, B[0].nmap, s);
+    launch_depth_level0(src, is_u16, pitch, scale, tr->cam[0], depth_m, B[0].invd, B[0].z, B[0].vmap, B[0].nmap,
+                        s);
     for (int l = 1; l < tr->L; ++l)
-        launch_depth_level(B[l - 1].invd, tr->cam[l - 1].w, tr->cam[l], B[l].invd, B[l].vmap, B[l].nmap, s);
+        launch_depth_level(B[l - 1].invd, tr->cam[l - 1].w, tr->cam[l], B[l].invd, B[l].z, B[l].vmap, B[l].nmap,
+                           s);
 }
 
 void tracker_model(yas_tracker *tr, cudaStream_t s) {

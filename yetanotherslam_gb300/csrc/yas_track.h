@@ -55,8 +55,8 @@ struct FusedLevel {
     LevelCam c;
     int iters;
     int chunk;  // pixels per CTA (a multiple of 32)
-    int pix;    // pixels per thread, ceil(chunk / kFusedThreads)
-    const float *ref_int, *ref_invd;
+    int pix;    // pixels per thread, ceil(chunk / threads per CTA)
+    const float *ref_int, *ref_invd, *ref_z;
     const float4 *ref_vmap, *ref_nmap;
     const float *cur_int, *cur_gx, *cur_gy;
     const float4 *cur_vmap, *cur_nmap;
@@ -77,6 +77,7 @@ struct GNBatchItem {
 struct TrackLevelBufs {
     float *intensity;
     float *invd;
+    float *z;  // 1 / invd where invd > 0, else 0: the depth the photometric warp uses
     float4 *vmap;
     float4 *nmap;
 };
@@ -86,8 +87,8 @@ void launch_image_level0(const uint8_t *src, int channels, int bgr, int pitch, i
 void launch_image_level(const float *prev, int pw, int ph, int w, int h, float *inten, float *gx, float *gy,
                         cudaStream_t s);
 void launch_depth_level0(const void *src, int is_u16, int pitch, float scale, const LevelCam &c,
-                         float *depth_m, float *invd, float4 *vmap, float4 *nmap, cudaStream_t s);
-void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float4 *vmap,
+                         float *depth_m, float *invd, float *zmap, float4 *vmap, float4 *nmap, cudaStream_t s);
+void launch_depth_level(const float *prev, int pw, const LevelCam &c, float *invd, float *zmap, float4 *vmap,
                         float4 *nmap, cudaStream_t s);
 void launch_model_pyramid(int L, const int *w, const int *h, float4 *const *vmap, float4 *const *nmap,
                           cudaStream_t s);
