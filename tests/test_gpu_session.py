@@ -102,6 +102,51 @@ def test_device_resident_inputs(cuda):
         assert np.array_equal(A, B)
 
 
+def test_frame_inputs_through_every_copy_path(cuda):
+    """A captured frame reads device and pinned host inputs through its own
+    copy node, re-pointed before each launch (and left alone when a buffer is
+    reused in place); pageable or unaligned inputs are copied on the stream
+    first.  Every mix, on both graph parities, gives the poses of a session fed
+    pageable host arrays, bit for bit."""
+    import torch
+
+    kinds = [0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 4, 4, 4]
+    W, H, n = 160, 120, len(kinds)
+    K = synth.intrinsics(W, H)
+    seq = sequence(3, n, W, H)
+    kw = dict(hash_slots=1 << 16, max_blocks=1 << 14)
+    s1 = rf.Session(W, H, K, **kw)
+    s2 = rf.Session(W, H, K, **kw)
+    keep_r = torch.empty(H, W, 3, dtype=torch.uint8, device="cuda")
+    keep_d = torch.empty(H, W, dtype=torch.int16, device="cuda")
+    for i, (rgb, d16, _, _) in enumerate(seq):
+        _, A = s1.process(rgb, d16)
+        kind = kinds[i]
+        if kind == 0:  # device tensors, fresh each frame
+            r = torch.from_numpy(rgb).cuda()
+            d = torch.from_numpy(d16.view(np.int16)).cuda()
+        elif kind == 1:  # pinned host memory
+            r = torch.from_numpy(rgb).pin_memory().numpy()
+            d = torch.from_numpy(d16.view(np.int16)).pin_memory().numpy().view(np.uint16)
+        elif kind == 2:  # pageable host memory
+            r, d = rgb, d16
+        elif kind == 3:  # device tensors 1 and 2 bytes off a 16-byte boundary
+            br = torch.empty(rgb.size + 16, dtype=torch.uint8, device="cuda")
+            bd = torch.empty(d16.size + 8, dtype=torch.int16, device="cuda")
+            r = br[1:1 + rgb.size].view(H, W, 3)
+            d = bd[1:1 + d16.size].view(H, W)
+            r.copy_(torch.from_numpy(rgb))
+            d.copy_(torch.from_numpy(d16.view(np.int16)))
+        else:  # one device buffer pair, overwritten in place
+            keep_r.copy_(torch.from_numpy(rgb))
+            keep_d.copy_(torch.from_numpy(d16.view(np.int16)))
+            r, d = keep_r, keep_d
+        torch.cuda.synchronize()
+        st, B = s2.process(r, d)
+        assert st == 0
+        assert np.array_equal(A, B), f"frame {i} (input kind {kind})"
+
+
 def test_lost_frame_is_rejected_and_map_unchanged(cuda):
     """A frame far from the previous one trips the 0.1 m step check
     (Tracking.cpp:178-184): no fusion, pose kept."""

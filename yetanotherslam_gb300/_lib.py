@@ -259,5 +259,5 @@ def pose_from(mat) -> Pose:
 def pose_to(p: Pose):
     import numpy as np
     out = np.eye(4)
-    out[:3, :4] = np.array(list(p.m), dtype=np.float64).reshape(3, 4)
+    out[:3, :4] = np.frombuffer(p.m, dtype=np.float64).reshape(3, 4)
     return out

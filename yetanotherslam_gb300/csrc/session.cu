@@ -126,6 +126,23 @@ __global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float m
     }
 }
 
+// A frame's input copy, the first node of a captured frame's frame branch: the
+// caller's rgb and depth (device memory, or pinned host memory the device
+// maps) into the session's buffers, 16 bytes per thread.  Its sources are set
+// on the node before every launch, so the copy runs beside the raycast branch
+// instead of ahead of the whole frame.  n_rgb = n_depth = 0 (the copies ran on
+// the stream before the launch) makes it return at once.
+__global__ void __launch_bounds__(256) input_copy_kernel(const uint4 *__restrict__ rgb,
+                                                         const uint4 *__restrict__ depth, uint4 *__restrict__ d_rgb,
+                                                         uint4 *__restrict__ d_depth, unsigned n_rgb,
+                                                         unsigned n_depth) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_rgb)
+        d_rgb[i] = rgb[i];
+    else if (i - n_rgb < n_depth)
+        d_depth[i - n_rgb] = depth[i - n_rgb];
+}
+
 }  // namespace yas
 
 using namespace yas;
@@ -148,6 +165,13 @@ struct yas_session {
     FrameState *fs_host = nullptr;
     int frames = 0;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    // the graphs exec[] came from, kept for their input-copy nodes, which are
+    // updated before every launch (null node: the copies run on the stream)
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphNode_t input_node[2] = {nullptr, nullptr};
+    const void *input_src[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // the nodes' current sources
+    bool capture_input = false;  // capturing exec[]: the frame branch starts with the input copy
+    int device = 0;
     cudaGraphExec_t pre_exec[2] = {nullptr, nullptr};  // served frames: up to the GN schedule
     cudaGraphExec_t post_exec = nullptr;               // served frames: after it
     // the map's device arrays when the graphs were captured: growth, fusion
@@ -242,8 +266,11 @@ static void enqueue_raycast_branch(yas_session *s, cudaStream_t st) {
 
 // Pyramids of the new frame (Tracking.cpp:172-173): read the frame, write the
 // current set and the float depth only.
+static void launch_input_copy(yas_session *s, cudaStream_t st);
+
 static void enqueue_frame_branch(yas_session *s, cudaStream_t st) {
     yas_tracker *tr = s->tr;
+    if (s->capture_input) launch_input_copy(s, st);
     prof_mark(s, kStImage);
     tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, false, st);
     prof_mark(s, kStDepth);
@@ -307,8 +334,10 @@ static int count_kernel_nodes(cudaGraph_t g, int *out) {
 }
 
 // Captures `fn` on the session stream into an executable graph; `kernels`
-// (optional) receives its count of kernel nodes.
-static int capture_graph(yas_session *s, void (*fn)(yas_session *), cudaGraphExec_t *out, int *kernels) {
+// (optional) receives its count of kernel nodes, `keep` (optional) the graph
+// itself (destroyed otherwise).
+static int capture_graph(yas_session *s, void (*fn)(yas_session *), cudaGraphExec_t *out, int *kernels,
+                         cudaGraph_t *keep = nullptr) {
     cudaGraph_t g = nullptr;
     YAS_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     fn(s);
@@ -326,12 +355,94 @@ static int capture_graph(yas_session *s, void (*fn)(yas_session *), cudaGraphExe
             st = YAS_ERR_CUDA;
         }
     }
-    cudaGraphDestroy(g);
+    if (st == YAS_OK && keep)
+        *keep = g;
+    else
+        cudaGraphDestroy(g);
     return st;
 }
 
+// ---------------------------------------------------------------- frame input
+static unsigned input_words(const yas_session *s) { return (unsigned)((size_t)s->cfg.width * s->cfg.height * 5 / 16); }
+
+static cudaKernelNodeParams input_params(yas_session *s, const void **src, void **args, unsigned *n) {
+    const size_t px = (size_t)s->cfg.width * s->cfg.height;
+    n[0] = src[0] ? (unsigned)(px * 3 / 16) : 0u;
+    n[1] = src[0] ? (unsigned)(px * 2 / 16) : 0u;
+    args[0] = &src[0];
+    args[1] = &src[1];
+    args[2] = &s->d_rgb;
+    args[3] = &s->d_depth;
+    args[4] = &n[0];
+    args[5] = &n[1];
+    cudaKernelNodeParams p = {};
+    p.func = (void *)input_copy_kernel;
+    p.gridDim = dim3((input_words(s) + 255) / 256);
+    p.blockDim = dim3(256);
+    p.sharedMemBytes = 0;
+    p.kernelParams = args;
+    p.extra = nullptr;
+    return p;
+}
+
+// The input copy node as captured: no sources (set before each launch).
+static void launch_input_copy(yas_session *s, cudaStream_t st) {
+    const uint4 *none = nullptr;
+    input_copy_kernel<<<(input_words(s) + 255) / 256, 256, 0, st>>>(none, none, reinterpret_cast<uint4 *>(s->d_rgb),
+                                                                   reinterpret_cast<uint4 *>(s->d_depth), 0u, 0u);
+}
+
+// Device address of `bytes` of a frame input the input copy kernel can read:
+// 16-byte aligned memory of this device (on_device) or pinned host memory the
+// device maps; null otherwise (the copy then runs on the stream).
+static const void *readable_input(const yas_session *s, const void *p, size_t bytes, int on_device) {
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) || (bytes & 15u)) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const bool ok = on_device ? (a.type == cudaMemoryTypeDevice && a.device == s->device)
+                              : a.type == cudaMemoryTypeHost;
+    return ok ? a.devicePointer : nullptr;
+}
+
+// Points the input copy node of exec[parity] at this frame's sources (null:
+// the copies were enqueued on the stream and the node does nothing).
+static int set_input_node(yas_session *s, int parity, const void *rgb, const void *depth) {
+    if (s->input_src[parity][0] == rgb && s->input_src[parity][1] == depth) return YAS_OK;
+    const void *src[2] = {rgb, depth};
+    void *args[6];
+    unsigned n[2];
+    const cudaKernelNodeParams p = input_params(s, src, args, n);
+    YAS_TRY_CUDA(cudaGraphExecKernelNodeSetParams(s->exec[parity], s->input_node[parity], &p));
+    s->input_src[parity][0] = rgb;
+    s->input_src[parity][1] = depth;
+    return YAS_OK;
+}
+
 static int build_graph(yas_session *s, int parity) {
-    return capture_graph(s, enqueue_tracked_frame, &s->exec[parity], &s->kernels_per_frame);
+    s->capture_input = true;
+    cudaGraph_t g = nullptr;
+    const int st = capture_graph(s, enqueue_tracked_frame, &s->exec[parity], &s->kernels_per_frame, &g);
+    s->capture_input = false;
+    if (st != YAS_OK) return st;
+    s->graph[parity] = g;
+    s->input_node[parity] = nullptr;
+    s->input_src[parity][0] = s->input_src[parity][1] = nullptr;
+    size_t n = 0;
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    YAS_TRY_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        YAS_TRY_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+        if (t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p;
+        YAS_TRY_CUDA(cudaGraphKernelNodeGetParams(nodes[i], &p));
+        if (p.func == (void *)input_copy_kernel) s->input_node[parity] = nodes[i];
+    }
+    return YAS_OK;
 }
 
 // ---------------------------------------------------------------- interface for the request server
@@ -350,8 +461,11 @@ bool session_needs_init(const yas_session *s) { return s->frames == 0; }
 static void drop_graphs(yas_session *s) {
     for (int i = 0; i < 2; ++i) {
         if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+        if (s->graph[i]) cudaGraphDestroy(s->graph[i]);
         if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
         s->exec[i] = s->pre_exec[i] = nullptr;
+        s->graph[i] = nullptr;
+        s->input_node[i] = nullptr;
     }
     if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
     s->post_exec = nullptr;
@@ -462,6 +576,11 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
     *out = nullptr;
     yas_session *s = new yas_session();
     s->cfg = *cfg;
+    if (cudaGetDevice(&s->device) != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return YAS_ERR_CUDA;
+    }
     if (stream) {
         s->stream = (cudaStream_t)stream;
     } else {
@@ -531,11 +650,7 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
 YAS_API int yas_session_destroy(yas_session *s) {
     if (!s) return YAS_ERR_BAD_ARG;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (int i = 0; i < 2; ++i) {
-        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
-        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
-    }
-    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
+    drop_graphs(s);
     if (s->tr) yas_tracker_destroy(s->tr);
     if (s->rc) yas_raycaster_destroy(s->rc);
     cudaFree(s->zt.znear);
@@ -564,15 +679,32 @@ YAS_API int yas_session_submit(yas_session *s, const uint8_t *rgb, const uint16_
     YAS_TRY(check_graphs(s));
     const size_t n = (size_t)s->cfg.width * s->cfg.height;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (s->frames > 0 && s->cfg.use_graph) {
+        const int parity = s->tr->cur;
+        if (!s->exec[parity]) YAS_TRY(build_graph(s, parity));
+        // the graph's own input copy reads the sources where it can (off the
+        // raycast's path); otherwise they are copied on the stream first
+        const void *src_rgb = nullptr, *src_depth = nullptr;
+        if (s->input_node[parity]) {
+            src_rgb = readable_input(s, rgb, n * 3, on_device);
+            src_depth = src_rgb ? readable_input(s, depth, n * 2, on_device) : nullptr;
+            if (!src_depth) src_rgb = nullptr;
+            YAS_TRY(set_input_node(s, parity, src_rgb, src_depth));
+        }
+        if (!src_rgb) {
+            YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
+            YAS_TRY_CUDA(cudaMemcpyAsync(s->d_depth, depth, n * 2, kind, s->stream));
+        }
+        YAS_TRY_CUDA(cudaGraphLaunch(s->exec[parity], s->stream));
+        s->tr->cur = 1 - s->tr->cur;
+        YAS_TRY_CUDA(cudaGetLastError());
+        s->frames++;
+        return YAS_OK;
+    }
     YAS_TRY_CUDA(cudaMemcpyAsync(s->d_rgb, rgb, n * 3, kind, s->stream));
     YAS_TRY_CUDA(cudaMemcpyAsync(s->d_depth, depth, n * 2, kind, s->stream));
     if (s->frames == 0) {
         enqueue_first_frame(s);
-    } else if (s->cfg.use_graph) {
-        const int parity = s->tr->cur;
-        if (!s->exec[parity]) YAS_TRY(build_graph(s, parity));
-        YAS_TRY_CUDA(cudaGraphLaunch(s->exec[parity], s->stream));
-        s->tr->cur = 1 - s->tr->cur;
     } else {
         enqueue_tracked_frame(s);
         s->tr->cur = 1 - s->tr->cur;
@@ -632,13 +764,7 @@ YAS_API int yas_session_new_submap(yas_session *s, yas_map **out_previous) {
     *out_previous = s->map;
     s->map = nm;
     // captured frames name the previous map's arrays: capture again
-    for (int i = 0; i < 2; ++i) {
-        if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
-        if (s->pre_exec[i]) cudaGraphExecDestroy(s->pre_exec[i]);
-        s->exec[i] = s->pre_exec[i] = nullptr;
-    }
-    if (s->post_exec) cudaGraphExecDestroy(s->post_exec);
-    s->post_exec = nullptr;
+    drop_graphs(s);
     // the frame's pose relative to the new submap restarts at the identity;
     // the next raycast's z-range tiles are the new (empty) map's
     frame_begin_kernel<<<1, 32, 0, s->stream>>>(s->fs, pose_identity(), nm->hdr);

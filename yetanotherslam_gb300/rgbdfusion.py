@@ -10,6 +10,8 @@ Every call goes to ``libyas_gb300``; there is no Python fallback.
 from __future__ import annotations
 
 import ctypes as C
+import math
+import sys
 
 import numpy as np
 
@@ -29,14 +31,23 @@ def _intr(K) -> L.Intrinsics:
 
 
 def _device_info(a):
-    """(pointer, pitch_bytes, on_device) of an image argument."""
+    """(pointer, pitch_bytes, on_device, object to keep alive) of an image argument."""
+    torch = sys.modules.get("torch")
+    if torch is not None and isinstance(a, torch.Tensor) and a.is_cuda:
+        # the tensor's own accessors: building its __cuda_array_interface__
+        # dict costs several microseconds per image and frame
+        if a.requires_grad:
+            a = a.detach()
+        es = a.element_size()
+        row = math.prod(a.shape[1:]) * es if a.is_contiguous() else a.stride(0) * es
+        return a.data_ptr(), row, 1, a
     cai = getattr(a, "__cuda_array_interface__", None)
     if cai is not None:
         ptr = cai["data"][0]
         shape = cai["shape"]
         strides = cai.get("strides")
         itemsize = np.dtype(cai["typestr"]).itemsize
-        row = strides[0] if strides else int(np.prod(shape[1:])) * itemsize
+        row = strides[0] if strides else math.prod(shape[1:]) * itemsize
         return ptr, row, 1, a
     arr = np.ascontiguousarray(a)
     return arr.ctypes.data, arr.strides[0], 0, arr
@@ -435,6 +446,10 @@ class Session:
         self.width, self.height = width, height
         self.handle = C.c_void_p()
         L.call("yas_session_create", C.byref(self.handle), C.byref(cfg), stream)
+        # per-frame calls, looked up once
+        lib = L.load()
+        self._submit_fn, self._wait_fn = lib.yas_session_submit, lib.yas_session_wait
+        self._pose, self._status = L.Pose(), C.c_int()
 
     def close(self):
         if self.handle:
@@ -453,13 +468,11 @@ class Session:
         if rdev != ddev:
             raise ValueError("rgb and depth must both be host or both be device arrays")
         self._keep = (k1, k2)
-        L.call("yas_session_submit", self.handle, rp, dp, rdev)
+        L.check(self._submit_fn(self.handle, rp, dp, rdev), "yas_session_submit")
 
     def wait(self):
-        p = L.Pose()
-        st = C.c_int()
-        L.call("yas_session_wait", self.handle, C.byref(p), C.byref(st))
-        return st.value, L.pose_to(p)
+        L.check(self._wait_fn(self.handle, C.byref(self._pose), C.byref(self._status)), "yas_session_wait")
+        return self._status.value, L.pose_to(self._pose)
 
     def process(self, rgb, depth):
         """Tracks and fuses one frame; returns (status, Tcm 4x4)."""
