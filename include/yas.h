@@ -439,8 +439,11 @@ YAS_API int yas_session_config_default(yas_session_config *cfg, int width, int h
 YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg, void *stream);
 YAS_API int yas_session_destroy(yas_session *s);
 /* Enqueues one frame (RGB u8 interleaved w*h*3, depth u16 w*h) without waiting.
- * Inputs on the host must stay valid until yas_session_wait returns; they are
- * copied to the device on the session stream. */
+ * Inputs (host or device) must stay valid and unchanged until yas_session_wait
+ * returns.  A tracked frame's graph reads 16-byte-aligned device memory of the
+ * session's GPU or pinned host memory itself, beside the raycast; other inputs
+ * are first copied on the session stream.  Either way the frame reads exactly
+ * w*h*3 and w*h*2 bytes. */
 YAS_API int yas_session_submit(yas_session *s, const uint8_t *rgb, const uint16_t *depth,
                                int on_device);
 /* Waits for the last submitted frame; returns its map pose Tcm and frame status
