@@ -83,10 +83,29 @@ struct BlockLine {
 
 constexpr int kMaxLineBlocks = 1024;
 
+// Launches `k` on `s`; `dependent`: as a programmatic dependent of the
+// previous kernel on `s` (the kernel calls dependent_wait() first).
+template <typename... P, typename... A>
+static void launch_kernel(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, bool dependent, A... args) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.dynamicSmemBytes = 0;
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = dependent ? 1 : 0;
+    cudaLaunchKernelEx(&c, k, args...);
+}
+
 template <int VBYTES>
 __global__ void __launch_bounds__(256) allocate_kernel(MapDev m, const float *__restrict__ depth,
                                                        int pitch, Cam cam, const PosePair *P,
                                                        const int *skip) {
+    dependent_wait();
+    release_dependents();
     if (skip && *skip) return;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -131,13 +150,11 @@ __global__ void __launch_bounds__(256) allocate_kernel(MapDev m, const float *__
 }
 
 void launch_allocate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                     const PosePair *P, const int *skip, cudaStream_t s) {
+                     const PosePair *P, const int *skip, cudaStream_t s, bool dependent) {
     dim3 block(256);
     dim3 grid((cam.w + 31) / 32, (cam.h + 7) / 8);
-    if (fmt == YAS_VOXEL_F32)
-        allocate_kernel<8><<<grid, block, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
-    else
-        allocate_kernel<4><<<grid, block, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+    launch_kernel(fmt == YAS_VOXEL_F32 ? allocate_kernel<8> : allocate_kernel<4>, grid, block, s, dependent, m,
+                  depth, pitch_elems, cam, P, skip);
 }
 
 // ---------------------------------------------------------------- visibility
@@ -162,6 +179,8 @@ __device__ __forceinline__ bool block_visible(const Cam &c, const Rigid32 &Tinv,
 
 __global__ void __launch_bounds__(256) visible_kernel(MapDev m, Cam cam, const PosePair *P,
                                                       const int *skip) {
+    dependent_wait();
+    release_dependents();
     if (skip && *skip) return;
     const unsigned n = num_blocks(m);
     const Rigid32 Tinv = P->Tinv;
@@ -180,8 +199,8 @@ __global__ void __launch_bounds__(256) visible_kernel(MapDev m, Cam cam, const P
 }
 
 void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const int *skip,
-                    cudaStream_t s) {
-    visible_kernel<<<kSMs * 4, 256, 0, s>>>(m, cam, P, skip);
+                    cudaStream_t s, bool dependent) {
+    launch_kernel(visible_kernel, dim3(kSMs * 4), dim3(256), s, dependent, m, cam, P, skip);
 }
 
 // ---------------------------------------------------------------- integration
@@ -210,6 +229,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
                                                         const int *skip) {
     typedef VoxelIO<FMT> IO;
     typedef typename IO::T V;
+    dependent_wait();
     if (skip && *skip) return;
     const unsigned nvis = *(volatile unsigned *)&m.hdr->n_visible;
     const Rigid32 Tinv = P->Tinv;
@@ -299,27 +319,32 @@ __global__ void __launch_bounds__(256) integrate_kernel(MapDev m, const float *_
 
 template <int SIGN>
 static void launch_integrate_sign(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                                  const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0) {
-    const int grid = grid_ctas > 0 ? grid_ctas : kSMs * 8;
+                                  const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0,
+                                  bool dependent = false) {
+    const dim3 grid(grid_ctas > 0 ? grid_ctas : kSMs * 8);
     switch (fmt) {
         case YAS_VOXEL_F32:
-            integrate_kernel<YAS_VOXEL_F32, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            launch_kernel(integrate_kernel<YAS_VOXEL_F32, SIGN>, grid, dim3(256), s, dependent, m, depth, pitch_elems,
+                          cam, P, skip);
             break;
         case YAS_VOXEL_F16:
-            integrate_kernel<YAS_VOXEL_F16, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            launch_kernel(integrate_kernel<YAS_VOXEL_F16, SIGN>, grid, dim3(256), s, dependent, m, depth, pitch_elems,
+                          cam, P, skip);
             break;
         case YAS_VOXEL_S16:
-            integrate_kernel<YAS_VOXEL_S16, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            launch_kernel(integrate_kernel<YAS_VOXEL_S16, SIGN>, grid, dim3(256), s, dependent, m, depth, pitch_elems,
+                          cam, P, skip);
             break;
         default:
-            integrate_kernel<YAS_VOXEL_S24, SIGN><<<grid, 256, 0, s>>>(m, depth, pitch_elems, cam, P, skip);
+            launch_kernel(integrate_kernel<YAS_VOXEL_S24, SIGN>, grid, dim3(256), s, dependent, m, depth, pitch_elems,
+                          cam, P, skip);
             break;
     }
 }
 
 void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas) {
-    launch_integrate_sign<1>(m, fmt, depth, pitch_elems, cam, P, skip, s, grid_ctas);
+                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas, bool dependent) {
+    launch_integrate_sign<1>(m, fmt, depth, pitch_elems, cam, P, skip, s, grid_ctas, dependent);
 }
 
 void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,

@@ -78,10 +78,21 @@ __global__ void frame_begin_kernel(FrameState *fs, Pose64 init, MapHeader *hdr) 
     }
 }
 
+// The frame state into the host's pinned copy (mapped memory; the host reads
+// it once the stream is synchronised), one warp.
+__device__ __forceinline__ void frame_state_to_host(const FrameState *fs, FrameState *host, int lane) {
+    __syncwarp();
+    const unsigned *src = reinterpret_cast<const unsigned *>(fs);
+    unsigned *dst = reinterpret_cast<unsigned *>(host);
+    for (int i = lane; i < (int)(sizeof(FrameState) / 4); i += 32) dst[i] = src[i];
+}
+
 // Frame-step check and pose composition: Tcm <- Tcm * DT^-1 (Tracking.cpp:178-187),
 // one warp, one lane per matrix entry (FP64 issues at the same cost for one or
-// 32 active lanes on GB300).
-__global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float max_t, MapHeader *hdr) {
+// 32 active lanes on GB300); the result also goes to the host's copy.
+__global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float max_t, MapHeader *hdr,
+                                      FrameState *host) {
+    release_dependents();
     const int lane = threadIdx.x;
     __shared__ double Di[12], A[12];
     __shared__ int ok;
@@ -103,7 +114,10 @@ __global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float m
     }
     __syncwarp();
     if (!st->failed && lane < 12) fs->dt[lane] = D[lane];
-    if (!ok) return;
+    if (!ok) {
+        frame_state_to_host(fs, host, lane);
+        return;
+    }
     if (lane < 12) {
         // DT^-1 = [R^T | -R^T t]
         const int i = lane / 4, j = lane % 4;
@@ -124,6 +138,7 @@ __global__ void frame_finalize_kernel(FrameState *fs, const GNState *st, float m
         fs->status = YAS_OK;
         hdr->n_visible = 0;
     }
+    frame_state_to_host(fs, host, lane);
 }
 
 // A frame's input copy, the first node of a captured frame's frame branch: the
@@ -163,6 +178,7 @@ struct yas_session {
     float *d_depth_m = nullptr;
     FrameState *fs = nullptr;
     FrameState *fs_host = nullptr;
+    FrameState *fs_host_dev = nullptr;  // fs_host as the device maps it
     int frames = 0;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     // the graphs exec[] came from, kept for their input-copy nodes, which are
@@ -217,14 +233,17 @@ static void enqueue_zrange(yas_session *s, cudaStream_t st) {
 // Allocation, visibility and integration (Fuse, VoxelMap.cu:517-786), then the
 // next frame's z-range tiles: beside integration on the side stream (they
 // need only the visible list and the pose), after it when profiling.
-static void enqueue_fusion(yas_session *s, const int *skip) {
+// `dependent`: each of the three kernels is a programmatic dependent of the
+// one before it (the frame step before allocation), except when profiling.
+static void enqueue_fusion(yas_session *s, const int *skip, bool dependent) {
     MapDev v = map_view(s->map);
     const int fmt = s->map->cfg.voxel_format;
     cudaStream_t st = s->stream;
+    dependent = dependent && !s->profiling;
     prof_mark(s, kStAllocate);
-    launch_allocate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st);
+    launch_allocate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st, dependent);
     prof_mark(s, kStVisible);
-    launch_visible(v, s->cam, &s->fs->pp, skip, st);
+    launch_visible(v, s->cam, &s->fs->pp, skip, st, dependent);
     const bool side = s->side && !s->profiling;
     if (side) {
         cudaEventRecord(s->ev_fork, st);
@@ -232,7 +251,8 @@ static void enqueue_fusion(yas_session *s, const int *skip) {
         enqueue_zrange(s, s->side);
     }
     prof_mark(s, kStIntegrate);
-    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st, s->shape.integrate_ctas);
+    launch_integrate(v, fmt, s->d_depth_m, s->cfg.width, s->cam, &s->fs->pp, skip, st, s->shape.integrate_ctas,
+                     dependent);
     if (side) {
         cudaEventRecord(s->ev_join, s->side);
         cudaStreamWaitEvent(st, s->ev_join, 0);
@@ -246,7 +266,7 @@ static void enqueue_first_frame(yas_session *s) {
     tracker_image(tr, s->d_rgb, 3, s->cfg.width * 3, true, s->stream);
     tracker_depth(tr, s->d_depth, 1, s->cfg.width * 2, s->cfg.depth_scale, s->d_depth_m, true, s->stream);
     frame_begin_kernel<<<1, 32, 0, s->stream>>>(s->fs, pose_identity(), s->map->hdr);
-    enqueue_fusion(s, nullptr);
+    enqueue_fusion(s, nullptr, false);
     cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, s->stream);
 }
 
@@ -301,15 +321,15 @@ static void enqueue_pre(yas_session *s) {
     }
 }
 
-// A tracked frame after the Gauss-Newton schedule: pose update, fusion, frame
-// state to the host.
+// A tracked frame after the Gauss-Newton schedule: pose update (its result
+// written to the host's copy too), fusion.
 static void enqueue_post(yas_session *s) {
     cudaStream_t st = s->stream;
     prof_mark(s, kStFinalize);
-    frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, s->tr->state, s->cfg.max_step_translation, s->map->hdr);
-    enqueue_fusion(s, &s->fs->skip);
+    frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, s->tr->state, s->cfg.max_step_translation, s->map->hdr,
+                                            s->fs_host_dev);
+    enqueue_fusion(s, &s->fs->skip, true);
     prof_mark(s, kStEnd);
-    cudaMemcpyAsync(s->fs_host, s->fs, sizeof(FrameState), cudaMemcpyDeviceToHost, st);
 }
 
 static void enqueue_tracked_frame(yas_session *s) {
@@ -620,7 +640,8 @@ YAS_API int yas_session_create(yas_session **out, const yas_session_config *cfg,
         const size_t n = (size_t)cfg->width * cfg->height;
         if (cudaMalloc(&s->d_rgb, n * 3) != cudaSuccess || cudaMalloc(&s->d_depth, n * 2) != cudaSuccess ||
             cudaMalloc(&s->d_depth_m, n * 4) != cudaSuccess || cudaMalloc(&s->fs, sizeof(FrameState)) != cudaSuccess ||
-            cudaMallocHost(&s->fs_host, sizeof(FrameState)) != cudaSuccess) {
+            cudaMallocHost(&s->fs_host, sizeof(FrameState)) != cudaSuccess ||
+            cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->fs_host_dev), s->fs_host, 0) != cudaSuccess) {
             cudaGetLastError();
             st = YAS_ERR_OOM;
         } else {

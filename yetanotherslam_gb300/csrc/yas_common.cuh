@@ -268,6 +268,16 @@ __device__ __forceinline__ void raise_error(const MapDev &m, int code) {
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Programmatic dependent launch.  A kernel launched as a dependent of the
+// previous kernel on its stream may be scheduled while that kernel still runs:
+// dependent_wait() returns once the previous kernel has completed and its
+// writes are visible, so a dependent calls it before its first memory access.
+// release_dependents() lets the next kernel's CTAs be scheduled (they still
+// wait for this one to complete).  Both do nothing in a kernel launched the
+// ordinary way.
+__device__ __forceinline__ void dependent_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void release_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned r;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));

@@ -64,16 +64,20 @@ int map_dev_alloc(yas_map *m);
 void map_dev_free(yas_map *m);
 MapDev map_view(const yas_map *m);
 
+// `dependent` (allocate, visible, integrate): launched as a programmatic
+// dependent of the previous kernel on `s`, which must be a kernel; its CTAs
+// are scheduled while that kernel finishes and wait for it in the kernel.
 // Allocates blocks along each depth ray (FP32-exact line tracing).
 void launch_allocate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                     const PosePair *P, const int *skip, cudaStream_t s);
+                     const PosePair *P, const int *skip, cudaStream_t s, bool dependent = false);
 // Compacts the visible blocks into m.visible; hdr->n_visible must be zero.
 void launch_visible(const MapDev &m, const Cam &cam, const PosePair *P, const int *skip,
-                    cudaStream_t s);
+                    cudaStream_t s, bool dependent = false);
 // Integrates depth into the visible blocks.
 // `grid_ctas` 0: the default grid (152 x 8 CTAs of 256 threads).
 void launch_integrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
-                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0);
+                      const PosePair *P, const int *skip, cudaStream_t s, int grid_ctas = 0,
+                      bool dependent = false);
 void launch_deintegrate(const MapDev &m, int fmt, const float *depth, int pitch_elems, const Cam &cam,
                         const PosePair *P, cudaStream_t s);
 // Submap fusion and growth (fusion.cu)
