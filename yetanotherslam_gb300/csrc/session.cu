@@ -322,20 +322,24 @@ static void enqueue_pre(yas_session *s) {
 }
 
 // A tracked frame after the Gauss-Newton schedule: pose update (its result
-// written to the host's copy too), fusion.
-static void enqueue_post(yas_session *s) {
+// written to the host's copy too), fusion.  `dependent`: the fusion kernels
+// are programmatic dependents (a lone session's frame; where sessions share
+// the GPU, their waiting CTAs would hold slots other sessions' kernels need).
+static void enqueue_post_as(yas_session *s, bool dependent) {
     cudaStream_t st = s->stream;
     prof_mark(s, kStFinalize);
     frame_finalize_kernel<<<1, 32, 0, st>>>(s->fs, s->tr->state, s->cfg.max_step_translation, s->map->hdr,
                                             s->fs_host_dev);
-    enqueue_fusion(s, &s->fs->skip, true);
+    enqueue_fusion(s, &s->fs->skip, dependent);
     prof_mark(s, kStEnd);
 }
+
+static void enqueue_post(yas_session *s) { enqueue_post_as(s, false); }
 
 static void enqueue_tracked_frame(yas_session *s) {
     enqueue_pre(s);
     launch_gn_schedule(s->tr, s->stream);
-    enqueue_post(s);
+    enqueue_post_as(s, true);
 }
 
 static int count_kernel_nodes(cudaGraph_t g, int *out) {
