@@ -56,6 +56,7 @@ WORKLOAD = {
     "l2": "GPU arm: flushed between steps (a 256 MB write outside the timed events)",
 }
 GPU_STORAGE = "fp16 sdf + u8 weight + fp16 rounding residual (4 B per voxel)"
+FRAME_STATE_BYTES = 304  # the session's per-frame state the host reads back (csrc/session.cu FrameState)
 
 
 def rank_max(x: float) -> float:
@@ -321,8 +322,11 @@ def run_gpu(args):
                   "frame_status_nonzero": int(sum(1 for x in statuses if x != 0)),
                   "stage_ms_per_frame": {stage_name(k): round(v, 4) for k, v in sorted(per_frame.items())},
                   "visible_blocks": nvis},
+        # in: the RGB and depth frame; out: the session's frame state (304 B: pose
+        # pair, Tcm, the frame step, status), written by the frame step into
+        # the host's mapped copy
         "e2e": {"value": round(whole_job_rate(world, args.steps, e2e_s), 2), "unit": "frames/s",
-                "h2d_bytes_per_step": W * H * 3 + W * H * 2, "d2h_bytes_per_step": 256},
+                "h2d_bytes_per_step": W * H * 3 + W * H * 2, "d2h_bytes_per_step": FRAME_STATE_BYTES},
         "gpu_launches": kernels * args.steps,
         "roofline": {"bound": "hbm", "kernel": stage_name(dom), "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
