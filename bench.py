@@ -9,12 +9,13 @@ path: image and depth pyramids, raycast of the map at the previous pose,
 model pyramid, 18 Gauss-Newton iterations with the device-side double-float solve,
 frame-step check, pose update, block allocation, visibility, integration.
 
-value: frames/s with the frame already in HBM (one device-to-device copy
-into the session plus the captured frame graph, timed with CUDA events on
-the session stream; L2 is flushed with a 256 MB write between steps, outside
-the timed events).  e2e: frames/s through the C ABI with host (pinned)
-buffers, the host-to-device upload and the pose read-back inside the timed
-region (wall clock around the synchronous process call).
+value: frames/s with the frame already in HBM (the captured frame graph,
+whose first node copies the frame into the session's buffers, timed with
+CUDA events on the session stream around the submit call; L2 is flushed
+with a 256 MB write between steps, outside the timed events).  e2e:
+frames/s through the C ABI with host (pinned) buffers, the graph reading
+the frame from host memory and the frame state written back to the host
+inside the timed region (wall clock around the synchronous process call).
 
 ``--impl reference`` times the CPU restatement of the reference's path
 (the oracle built in FP32 with OpenMP on every host core) on the same
